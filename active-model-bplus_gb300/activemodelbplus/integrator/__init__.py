@@ -1,0 +1,581 @@
+"""GB300-native drop-in for the reference's ``activemodelbplus.integrator``.
+
+Same public names and behaviour as the reference package
+(tranqui/active-model-bplus, ``activemodelbplus/integrator/__init__.py`` over the
+pybind11 module ``src/integrator.cc``): ``Model``, ``Stencil``, ``Integrator``
+(``run``, ``run_for_time``, ``field``, the current getters, ``time``,
+``timestep``), ``CudaException``, ``steps_from_time``, ``step_iterator`` and
+``plot_field``.
+
+Behind the API: device buffers are torch CUDA tensors, and every step is one
+launch of a hand-written sm_103a kernel in ``libamb_gb300.so`` (C ABI,
+include/amb_gb300.h) on the current torch stream. There is no CPU path.
+
+Additions with no reference counterpart (all keyword-only or new names):
+``precision`` ("f64" default, "f32", "f32c"), ``seed`` (Philox noise key; the
+reference seeds non-deterministically), ``kernel``, the chemical-potential
+getters the reference leaves unbound, ``mass()``, ``field_tensor``,
+``checkpoint()`` / ``Integrator.from_checkpoint()``, ``sample()``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+from . import _native as N
+
+__all__ = ["Model", "Stencil", "Integrator", "CudaException", "steps_from_time", "step_iterator", "plot_field"]
+
+
+class CudaException(RuntimeError):
+    """Raised on CUDA errors and on a non-finite field after ``run``
+    (the reference's ``kernel::CudaError``, src/integrator.h:10-14, src/integrator.cc:33)."""
+
+
+def _check(rc: int) -> None:
+    if rc == N.AMB_OK:
+        return
+    msg = N.last_error()
+    if rc == N.AMB_ERR_INVALID:
+        raise ValueError(msg)
+    raise CudaException(msg)
+
+
+# ------------------------------------------------------------------ parameters
+
+class Model:
+    """Active Model B+ parameters (src/parameters.h:54-77, bound at src/integrator.cc:35-72).
+
+    ``Model()``, ``Model(a, b, c, kappa, lamb, zeta, T)`` or ``Model(model)`` (copy).
+    ``as_dict()`` uses the key ``"temperature"`` for ``T`` as the reference does.
+    """
+    _names = ("a", "b", "c", "kappa", "lamb", "zeta", "T")
+    __slots__ = _names
+
+    def __init__(self, *args, **kwargs):
+        if len(args) == 1 and not kwargs and isinstance(args[0], Model):
+            vals = args[0].as_tuple()
+        elif not args and set(kwargs) == {"model"}:
+            vals = Model(kwargs["model"]).as_tuple()
+        else:
+            if len(args) > len(self._names):
+                raise TypeError("Model takes at most 7 parameters")
+            given = dict(zip(self._names, args))
+            for k, v in kwargs.items():
+                if k not in self._names or k in given:
+                    raise TypeError(f"unexpected or repeated argument {k!r}")
+                given[k] = v
+            vals = tuple(float(given.get(k, 0.0)) for k in self._names)
+        for k, v in zip(self._names, vals):
+            object.__setattr__(self, k, float(v))
+
+    def __setattr__(self, k, v):
+        if k not in self._names:
+            raise AttributeError(k)
+        object.__setattr__(self, k, float(v))
+
+    def as_tuple(self):
+        return tuple(getattr(self, k) for k in self._names)
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k in ("a", "b", "c", "kappa", "lamb", "zeta")}
+        d["temperature"] = self.T
+        return d
+
+    def __eq__(self, other):
+        return isinstance(other, Model) and self.as_tuple() == other.as_tuple()
+
+    __hash__ = None
+
+    def __str__(self):
+        return str(self.as_dict())
+
+    def __repr__(self):
+        return "<Model " + str(self.as_dict()) + ">"
+
+
+class Stencil:
+    """Discretisation parameters (src/parameters.h:23-41, bound at src/integrator.cc:74-103).
+
+    ``Stencil()``, ``Stencil(dt, dx, dy)`` or ``Stencil(stencil)`` (copy).
+    """
+    _names = ("dt", "dx", "dy")
+    __slots__ = _names
+
+    def __init__(self, *args, **kwargs):
+        if len(args) == 1 and not kwargs and isinstance(args[0], Stencil):
+            vals = args[0].as_tuple()
+        elif not args and set(kwargs) == {"stencil"}:
+            vals = Stencil(kwargs["stencil"]).as_tuple()
+        else:
+            if len(args) > 3:
+                raise TypeError("Stencil takes at most 3 parameters")
+            given = dict(zip(self._names, args))
+            for k, v in kwargs.items():
+                if k not in self._names or k in given:
+                    raise TypeError(f"unexpected or repeated argument {k!r}")
+                given[k] = v
+            vals = tuple(float(given.get(k, 0.0)) for k in self._names)
+        for k, v in zip(self._names, vals):
+            object.__setattr__(self, k, float(v))
+
+    def __setattr__(self, k, v):
+        if k not in self._names:
+            raise AttributeError(k)
+        object.__setattr__(self, k, float(v))
+
+    def as_tuple(self):
+        return tuple(getattr(self, k) for k in self._names)
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k in self._names}
+
+    def __eq__(self, other):
+        return isinstance(other, Stencil) and self.as_tuple() == other.as_tuple()
+
+    __hash__ = None
+
+    def __str__(self):
+        return str(self.as_dict())
+
+    def __repr__(self):
+        return "<Stencil " + str(self.as_dict()) + ">"
+
+
+# ------------------------------------------------------------------ integrator
+
+_PRECISIONS = {"f64": N.AMB_F64, "f32": N.AMB_F32, "f32c": N.AMB_F32C}
+_KERNELS = {"auto": N.AMB_KERNEL_AUTO, "tile": N.AMB_KERNEL_TILE, "sliding": N.AMB_KERNEL_SLIDING}
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _random_seed() -> int:
+    return int.from_bytes(os.urandom(8), "little")
+
+
+class Integrator:
+    """Explicit-Euler Active Model B+ integrator on one GPU
+    (the reference's ``Integrator``, src/integrator.h:24-81, src/integrator.cc:105-123).
+
+    Args:
+        field: initial field, array-like of shape (ny, nx) (axis 0 = y).
+        stencil: :class:`Stencil`.
+        model: :class:`Model`.
+        precision: "f64" (default; the reference's arithmetic), "f32" or "f32c"
+            (float field with a bf16 Kahan residual: compensated update).
+        seed: 64-bit key of the Philox noise; ``None`` draws one from the OS,
+            like the reference's non-deterministic seed.
+        device: CUDA device (default: current).
+        kernel: "auto", "tile" or "sliding" (FP32 kernel choice).
+    """
+
+    def __init__(self, field, stencil, model, *, precision: str = "f64", seed: int | None = None,
+                 device=None, kernel: str = "auto"):
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise CudaException("no CUDA device is available")
+        lib = N.lib()  # raises if the CUDA library is missing
+        if precision not in _PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}")
+        if kernel not in _KERNELS:
+            raise ValueError(f"kernel must be one of {sorted(_KERNELS)}")
+        host = np.asarray(field, dtype=np.float64)
+        if host.ndim != 2:
+            raise TypeError("field must be a 2D array (ny, nx)")
+        self._stencil = Stencil(stencil)
+        self._model = Model(model)
+        self._precision = precision
+        self._kernel = kernel
+        self._seed = _random_seed() if seed is None else int(seed) & 0xFFFFFFFFFFFFFFFF
+        self._device = torch.device("cuda", torch.cuda.current_device() if device is None else
+                                    torch.device(device).index or 0)
+        self._ny, self._nx = host.shape
+        if self._ny < 1 or self._nx < 1:
+            raise ValueError("field must have at least one site")
+        dtype = torch.float64 if precision == "f64" else torch.float32
+        self._buf = [torch.empty((self._ny, self._nx), dtype=dtype, device=self._device) for _ in range(2)]
+        self._cur = 0
+        self._residual = (torch.zeros((self._ny, self._nx), dtype=torch.int16, device=self._device)
+                          if precision == "f32c" else None)
+        self._flag = torch.zeros(1, dtype=torch.int32, device=self._device)
+        self._timestep = 0
+        self._terms_step = None
+        self._terms_dev = None
+        self._terms_host = None
+        self._events = None  # optional (start, end) CUDA events recorded around the step launches
+        self._s = N.stencil_struct(self._stencil)
+        self._m = N.model_struct(self._model)
+        self.set_field(host)
+        del lib
+
+    # -------------------------------------------------------------- plumbing
+    def _stream(self) -> int:
+        return _torch().cuda.current_stream(self._device).cuda_stream
+
+    @property
+    def field_tensor(self):
+        """The field as a device tensor (no copy; valid until the next ``run``)."""
+        return self._buf[self._cur]
+
+    def set_field(self, field) -> None:
+        """Replace the field (no reference counterpart; clears the residual)."""
+        torch = _torch()
+        host = np.asarray(field, dtype=np.float64)
+        if host.shape != (self._ny, self._nx):
+            raise ValueError(f"field shape {host.shape} != {(self._ny, self._nx)}")
+        self._buf[self._cur].copy_(torch.from_numpy(np.ascontiguousarray(host)))
+        if self._residual is not None:
+            self._residual.zero_()
+        self._terms_step = None
+
+    # ------------------------------------------------------------ reference API
+    @property
+    def stencil(self) -> Stencil:
+        return Stencil(self._stencil)
+
+    @property
+    def model(self) -> Model:
+        return Model(self._model)
+
+    @property
+    def timestep(self) -> int:
+        return self._timestep
+
+    @property
+    def time(self) -> float:
+        return self._timestep * self._stencil.dt
+
+    @property
+    def field(self) -> np.ndarray:
+        """A fresh float64 host copy of the field (src/integrator.cu:378-383)."""
+        return self._buf[self._cur].to(dtype=_torch().float64).cpu().numpy()
+
+    def run(self, nsteps: int) -> None:
+        """Advance ``nsteps`` explicit-Euler steps (src/integrator.cu:497-538).
+
+        Blocks until done and raises :class:`CudaException` if the field is no
+        longer finite. As in the reference, ``timestep`` advances by ``nsteps``
+        even when ``nsteps <= 0``.
+        """
+        nsteps = int(nsteps)
+        lib = N.lib()
+        stream = self._stream()
+        if nsteps > 0:
+            in_spare = ctypes.c_int(0)
+            cur, other = self._buf[self._cur], self._buf[1 - self._cur]
+            if self._events is not None:
+                self._events[0].record()
+            if self._precision == "f64":
+                rc = lib.amb_step_f64(ctypes.byref(self._s), ctypes.byref(self._m), self._seed, self._ny, self._nx,
+                                      cur.data_ptr(), other.data_ptr(), self._timestep, nsteps, None, stream,
+                                      ctypes.byref(in_spare))
+            else:
+                res = self._residual.data_ptr() if self._residual is not None else None
+                rc = lib.amb_step_f32(ctypes.byref(self._s), ctypes.byref(self._m), self._seed, self._ny, self._nx,
+                                      cur.data_ptr(), other.data_ptr(), res, self._timestep, nsteps, None,
+                                      _KERNELS[self._kernel], stream, ctypes.byref(in_spare))
+            if self._events is not None:
+                self._events[1].record()
+            _check(rc)
+            if in_spare.value:
+                self._cur = 1 - self._cur
+        self._timestep += nsteps
+        self._check_finite()
+
+    def _check_finite(self) -> None:
+        lib = N.lib()
+        f = self._buf[self._cur]
+        self._flag.zero_()
+        fn = lib.amb_check_finite_f64 if self._precision == "f64" else lib.amb_check_finite_f32
+        _check(fn(f.data_ptr(), f.numel(), self._flag.data_ptr(), self._stream()))
+        if int(self._flag.item()):
+            raise CudaException("an unknown numerical error occurred during simulation")
+
+    # ------------------------------------------------------------- getters
+    def _terms(self) -> np.ndarray:
+        """The ten FP64 term planes at the current timestep, cached per timestep
+        like the reference's lazy current recompute (src/integrator.cu:477-495)."""
+        if self._terms_step != self._timestep:
+            torch = _torch()
+            if self._terms_dev is None:
+                self._terms_dev = torch.empty((N.AMB_NTERMS, self._ny, self._nx), dtype=torch.float64,
+                                              device=self._device)
+            lib = N.lib()
+            fn = lib.amb_terms_f64 if self._precision == "f64" else lib.amb_terms_f32
+            _check(fn(ctypes.byref(self._s), ctypes.byref(self._m), self._seed, self._ny, self._nx,
+                      self._buf[self._cur].data_ptr(), self._timestep, None, self._terms_dev.data_ptr(),
+                      self._stream()))
+            self._terms_host = self._terms_dev.cpu().numpy()
+            self._terms_step = self._timestep
+        return self._terms_host
+
+    def _current(self, which: str):
+        t = self._terms()
+        out = []
+        for c in range(2):
+            jp, jl, jc, jr = t[2 + c], t[4 + c], t[6 + c], t[8 + c]
+            # sums in the reference's order (src/integrator.cu:406-465)
+            if which == "passive":
+                v = jp.copy()
+            elif which == "lambda":
+                v = jl.copy()
+            elif which == "circulating":
+                v = jc.copy()
+            elif which == "random":
+                v = jr.copy()
+            else:
+                active = jc + jl
+                if which == "active":
+                    v = active
+                else:
+                    det = active + jp
+                    v = det if which == "deterministic" else det + jr
+            out.append(v)
+        return out
+
+    @property
+    def current(self):
+        """Total current [J_y, J_x] (src/integrator.cu:406-412)."""
+        return self._current("total")
+
+    @property
+    def deterministic_current(self):
+        return self._current("deterministic")
+
+    @property
+    def passive_current(self):
+        return self._current("passive")
+
+    @property
+    def active_current(self):
+        return self._current("active")
+
+    @property
+    def lambda_current(self):
+        return self._current("lambda")
+
+    @property
+    def circulating_current(self):
+        return self._current("circulating")
+
+    @property
+    def random_current(self):
+        return self._current("random")
+
+    @property
+    def chemical_potential(self) -> np.ndarray:
+        """mu_p + mu_a (src/integrator.cu:385-388; not bound in the reference's module)."""
+        t = self._terms()
+        return t[0] + t[1]
+
+    @property
+    def passive_chemical_potential(self) -> np.ndarray:
+        return self._terms()[0].copy()
+
+    @property
+    def active_chemical_potential(self) -> np.ndarray:
+        return self._terms()[1].copy()
+
+    # ---------------------------------------------------------- additions
+    @property
+    def precision(self) -> str:
+        return self._precision
+
+    @property
+    def seed(self) -> int:
+        return self._seed
+
+    @property
+    def shape(self) -> tuple[int, int]:
+        return (self._ny, self._nx)
+
+    def mass(self) -> float:
+        """Sum of the field, FP64 with compensation, on the device."""
+        torch = _torch()
+        lib = N.lib()
+        f = self._buf[self._cur]
+        nbytes = lib.amb_mass_scratch_bytes(f.numel())
+        scratch = torch.empty(max(1, (nbytes + 7) // 8), dtype=torch.float64, device=self._device)
+        out = torch.empty(1, dtype=torch.float64, device=self._device)
+        fn = lib.amb_mass_f64 if self._precision == "f64" else lib.amb_mass_f32
+        _check(fn(f.data_ptr(), f.numel(), out.data_ptr(), scratch.data_ptr(), nbytes, self._stream()))
+        return float(out.item())
+
+    def checkpoint(self) -> dict:
+        """Everything needed to resume exactly: field (native dtype), residual, timestep, seed."""
+        d = {
+            "field": self._buf[self._cur].cpu().numpy().copy(),
+            "timestep": self._timestep,
+            "seed": self._seed,
+            "precision": self._precision,
+            "stencil": self._stencil.as_tuple(),
+            "model": self._model.as_tuple(),
+        }
+        if self._residual is not None:
+            d["residual"] = self._residual.cpu().numpy().copy()
+        return d
+
+    @classmethod
+    def from_checkpoint(cls, ckpt: dict, **kwargs) -> "Integrator":
+        torch = _torch()
+        sim = cls(np.asarray(ckpt["field"], dtype=np.float64), Stencil(*ckpt["stencil"]), Model(*ckpt["model"]),
+                  precision=ckpt["precision"], seed=int(ckpt["seed"]), **kwargs)
+        sim._buf[sim._cur].copy_(torch.from_numpy(np.ascontiguousarray(ckpt["field"])))
+        if sim._residual is not None and "residual" in ckpt:
+            sim._residual.copy_(torch.from_numpy(np.ascontiguousarray(ckpt["residual"])))
+        sim._timestep = int(ckpt["timestep"])
+        return sim
+
+    def save_checkpoint(self, path: str) -> None:
+        np.savez(path, **{k: np.asarray(v) for k, v in self.checkpoint().items()})
+
+    @classmethod
+    def load_checkpoint(cls, path: str, **kwargs) -> "Integrator":
+        z = np.load(path, allow_pickle=False)
+        d = {k: z[k] for k in z.files}
+        d["precision"] = str(d["precision"])
+        d["stencil"] = tuple(d["stencil"].tolist())
+        d["model"] = tuple(d["model"].tolist())
+        return cls.from_checkpoint(d, **kwargs)
+
+    # ---------------------------------------------------- run_for_time
+    def run_for_time(self, t, show_progress=False, t_interrupt=None, f_interrupt=None,
+                     max_updates=100, min_update_time=10):
+        """Run for simulation time ``t`` in chunks, calling ``f_interrupt(self)`` at
+        ``t_interrupt`` (activemodelbplus/integrator/__init__.py:105-161).
+
+        Raises:
+            ValueError: if ``t`` or an interrupt time is not a multiple of dt.
+        """
+        nsteps = steps_from_time(self.stencil.dt, t)
+        if t_interrupt is not None:
+            assert f_interrupt is not None
+            ti = np.asarray(t_interrupt)
+            if np.any(ti < 0) or np.any(ti > t):
+                raise ValueError("interrupt outside sim time window!")
+
+        initial_timestep = self.timestep
+        initial_time = self.time
+        plot = None
+        if show_progress:
+            plot = _ProgressPlot(self.field)
+
+        steps = step_iterator(self.stencil.dt, t, max_updates, min_update_time, t_interrupt=t_interrupt)
+        if show_progress:
+            steps = _progress(steps)
+
+        for n in steps:
+            if show_progress:
+                for out in (sys.stdout, sys.stderr):
+                    out.flush()
+            if t_interrupt is not None and np.any(np.isclose(self.time - initial_time, t_interrupt)):
+                f_interrupt(self)
+            assert n > 0
+            self.run(n)
+            if plot is not None:
+                plot.update(self.field)
+
+        if plot is not None:
+            plot.close()
+        assert (self.timestep - initial_timestep) == nsteps
+        if t_interrupt is not None and np.any(np.isclose(self.time - initial_time, t_interrupt)):
+            f_interrupt(self)
+
+
+# ------------------------------------------------------------------ helpers
+
+def steps_from_time(dt, tfinal):
+    """Number of steps to reach ``tfinal`` (activemodelbplus/integrator/__init__.py:39-57).
+
+    Raises:
+        ValueError: if ``tfinal`` is not a multiple of ``dt``.
+    """
+    nsteps = np.asarray(np.round(np.asarray(tfinal) / dt), dtype=int)
+    error = np.abs(nsteps - np.asarray(tfinal) / dt)
+    if not np.all(np.isclose(error, 0)):
+        raise ValueError(f"tfinal={tfinal} is not a multiple of dt={dt}!")
+    return nsteps.item() if nsteps.ndim == 0 else nsteps
+
+
+def step_iterator(dt, tfinal, max_updates, min_update_time, t_interrupt=None):
+    """Chunk sizes for a run of ``tfinal``: about even chunks, at most
+    ``max_updates`` of them, at least ``min_update_time`` apart, split at every
+    interrupt time (activemodelbplus/integrator/__init__.py:60-102)."""
+    min_steps = max(int(np.round(min_update_time / dt)), 1)
+    nsteps = steps_from_time(dt, tfinal)
+    nupdates = max(min(nsteps // min_steps, max_updates), 1)
+    timestep = np.linspace(0, nsteps, nupdates + 1, dtype=int)
+    if t_interrupt is not None:
+        interrupts = np.atleast_1d(steps_from_time(dt, np.asarray(t_interrupt).reshape(-1)))
+        timestep = np.unique(np.concatenate([timestep, interrupts]))
+    step_size = np.diff(timestep)
+    assert len(step_size) >= 1
+    assert np.sum(step_size) == nsteps
+    assert np.all(step_size >= 0)
+    return step_size
+
+
+def plot_field(field, fig=None, axes=None, fontsize=8):
+    """Draw (or redraw) the field with matplotlib (activemodelbplus/integrator/__init__.py:14-36).
+    matplotlib is imported only here."""
+    import matplotlib.pyplot as plt
+    from matplotlib.colors import Normalize
+
+    if fig is not None:
+        ax, im, cbar = axes
+        im.set_data(field)
+        im.set_norm(Normalize(field.min(), vmax=field.max()))
+        return fig, axes
+    fig = plt.figure()
+    ax = plt.gca()
+    im = ax.imshow(field)
+    cbar = fig.colorbar(im, ax=ax, fraction=0.05, pad=2e-2, location="right")
+    cbar.set_label(r"$\phi$", fontsize=fontsize)
+    cbar.ax.tick_params(labelsize=fontsize)
+    ax.set_xlabel("$x$", fontsize=fontsize)
+    ax.set_ylabel("$y$", fontsize=fontsize)
+    ax.set_xticks([])
+    ax.set_yticks([])
+    return fig, (ax, im, cbar)
+
+
+def _progress(it):
+    try:
+        from tqdm import tqdm
+    except ImportError:
+        return it
+    return tqdm(it)
+
+
+class _ProgressPlot:
+    """Live field display for run_for_time; a no-op when matplotlib/IPython are absent."""
+
+    def __init__(self, field):
+        try:
+            import matplotlib.pyplot  # noqa: F401
+            self.fig, self.axes = plot_field(field)
+        except ImportError:
+            self.fig = None
+
+    def update(self, field):
+        if self.fig is None:
+            return
+        plot_field(field, self.fig, self.axes)
+        try:
+            from IPython.display import clear_output, display
+            clear_output(wait=True)
+            display(self.fig)
+        except ImportError:
+            pass
+
+    def close(self):
+        if self.fig is not None:
+            import matplotlib.pyplot as plt
+            plt.close(self.fig)

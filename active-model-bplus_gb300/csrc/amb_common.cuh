@@ -1,0 +1,149 @@
+// Shared device-side definitions for the Active Model B+ step kernels:
+// per-launch parameters, the discrete operators, and the counter-based noise.
+//
+// Discrete operators (reference tranqui/active-model-bplus):
+//   D8   order-8 central first derivative, taps (1/280, -4/105, 1/5, -4/5, 0,
+//        4/5, -1/5, 4/105, -1/280) over offsets -4..4 (src/finite_difference.h:69-75);
+//        antisymmetric, applied here as sum_k d_k (g[+k] - g[-k]).
+//   Tj   Tjhung 3x3 first derivative [0.1, 0.3, 0.1] (smoothing, across) x
+//        [-1, 0, 1] (difference, along) (src/finite_difference.h:379-387,404-407).
+//   Lap  Tjhung Laplacian dxInv^2 [-.25, 1.5, -.25]_y x [1, -2, 1]_x +
+//        dyInv^2 [1, -2, 1]_y x [-.25, 1.5, -.25]_x (src/finite_difference.h:389-412,
+//        src/finite_difference.cuh:178-183).
+// All are applied in separable form; the rounding order therefore differs from
+// the reference's tap-by-tap sums, by O(1e-16) relative in FP64.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace amb
+{
+    // Everything one step needs, passed by value per launch (the reference keeps
+    // these in process-global __constant__ memory, src/parameters.cu:6-8).
+    struct StepParams
+    {
+        int ny, nx;                 // rows (y), cols (x)
+        double dt, dxInv, dyInv;
+        double a, b, c, kappa, lambda, zeta;
+        double noise_mag;           // sqrt(2T) sqrt(1/(dt dx dy)) (src/parameters.h:43-51,79-87)
+        uint64_t seed;
+        int64_t step;               // timestep whose currents drive the first update of the launch
+    };
+
+    // D8 antisymmetric taps d_1..d_4 (offset +k has +d_k, offset -k has -d_k).
+    __host__ __device__ constexpr double d8_tap(int k)
+    {
+        return k == 1 ? 4.0 / 5 : k == 2 ? -1.0 / 5 : k == 3 ? 4.0 / 105 : -1.0 / 280;
+    }
+
+    __host__ __device__ inline int wrap_index(long long i, int n)
+    {
+        long long r = i % n;
+        return int(r < 0 ? r + n : r);
+    }
+
+    // ------------------------------------------------------------ Philox noise
+
+    // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): ten rounds with the
+    // published multipliers and Weyl key increments.
+    struct U4 { uint32_t x, y, z, w; };
+
+    __device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1)
+    {
+        constexpr uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+        constexpr uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+        for (int round = 0; round < 10; ++round)
+        {
+            uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+            uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+            c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+            k0 += W0;
+            k1 += W1;
+        }
+        return c;
+    }
+
+    // Counter of the noise quad holding (row, col) for component comp (0 = y, 1 = x):
+    // (col >> 2, row, step mod 2^32, (step >> 32) << 1 | comp), key = seed.
+    __device__ __forceinline__ U4 noise_bits(uint64_t seed, int64_t step, int row, int col, int comp)
+    {
+        U4 ctr{uint32_t(col) >> 2, uint32_t(row), uint32_t(uint64_t(step)),
+               (uint32_t(uint64_t(step) >> 32) << 1) | uint32_t(comp)};
+        return philox4x32_10(ctr, uint32_t(seed), uint32_t(seed >> 32));
+    }
+
+    // Box-Muller on one pair of 32-bit words, 24-bit uniforms:
+    // ua = ((xa >> 8) + 1) 2^-24 in (0,1], ub = (xb >> 8) 2^-24 in [0,1);
+    // r = sqrt(-2 ln ua), theta = 2 pi (ub - 1/2); returns (r cos theta, r sin theta).
+    __device__ __forceinline__ double2 box_muller_f64(uint32_t xa, uint32_t xb)
+    {
+        double ua = (double((xa >> 8) + 1u)) * (1.0 / 16777216.0);
+        double ub = double(xb >> 8) * (1.0 / 16777216.0);
+        double r = sqrt(-2.0 * log(ua));
+        double s, c;
+        sincospi(2.0 * (ub - 0.5), &s, &c);
+        return make_double2(r * c, r * s);
+    }
+
+    // Single-precision counterpart of the same definition. -ln(ua) uses the fast
+    // hardware logarithm (__logf) where ua <= 31/32; closer to 1 its absolute
+    // error would rival ln(ua) itself, so there -ln(1 - v), v = 1 - ua (exact),
+    // is summed from the Mercator series v + v^2/2 + ... + v^5/5 (truncation
+    // below 1e-8 relative for v < 1/32). |theta| <= pi keeps __sincosf in its
+    // accurate range.
+    __device__ __forceinline__ float2 box_muller_f32(uint32_t xa, uint32_t xb)
+    {
+        uint32_t ka = xa >> 8;
+        float ua = float(ka + 1u) * (1.0f / 16777216.0f);
+        float v = float(16777215u - ka) * (1.0f / 16777216.0f);
+        float ub = float(xb >> 8) * (1.0f / 16777216.0f);
+        float t;
+        if (v < 0.03125f)
+            t = 2.0f * v * (1.0f + v * (0.5f + v * (0.333333343f + v * (0.25f + v * 0.2f))));
+        else
+            t = -2.0f * __logf(ua);
+        float r = t * rsqrtf(fmaxf(t, 1e-30f));
+        float s, c;
+        __sincosf(6.283185307179586f * (ub - 0.5f), &s, &c);
+        return make_float2(r * c, r * s);
+    }
+
+    // One standard normal of the (seed, step) noise field at (row, col, comp).
+    template <typename Real>
+    __device__ __forceinline__ Real noise_normal(uint64_t seed, int64_t step, int row, int col, int comp)
+    {
+        U4 q = noise_bits(seed, step, row, col, comp);
+        int lane = col & 3;
+        uint32_t xa = (lane < 2) ? q.x : q.z;
+        uint32_t xb = (lane < 2) ? q.y : q.w;
+        if constexpr (sizeof(Real) == 8)
+        {
+            double2 z = box_muller_f64(xa, xb);
+            return (lane & 1) ? z.y : z.x;
+        }
+        else
+        {
+            float2 z = box_muller_f32(xa, xb);
+            return (lane & 1) ? z.y : z.x;
+        }
+    }
+
+    // All four normals of a quad (columns 4q..4q+3).
+    template <typename Real>
+    __device__ __forceinline__ void noise_quad(uint64_t seed, int64_t step, int row, int col4, int comp, Real z[4])
+    {
+        U4 q = noise_bits(seed, step, row, col4, comp);
+        if constexpr (sizeof(Real) == 8)
+        {
+            double2 p0 = box_muller_f64(q.x, q.y), p1 = box_muller_f64(q.z, q.w);
+            z[0] = p0.x; z[1] = p0.y; z[2] = p1.x; z[3] = p1.y;
+        }
+        else
+        {
+            float2 p0 = box_muller_f32(q.x, q.y), p1 = box_muller_f32(q.z, q.w);
+            z[0] = p0.x; z[1] = p0.y; z[2] = p1.x; z[3] = p1.y;
+        }
+    }
+}

@@ -1,0 +1,36 @@
+// Internal launch interface between the C-ABI layer (amb_abi.cu) and the
+// kernel translation units. Not part of the public header.
+#pragma once
+
+#include "amb_common.cuh"
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace amb
+{
+    // Fused single-step tile kernel (amb_step_tile.cuh), one launch = one step.
+    template <typename Real>
+    cudaError_t launch_step_tile(const Real* phi_in, Real* phi_out, __nv_bfloat16* comp, int comp_mode,
+                                 const StepParams& p, int noise_mode, const Real* injected, cudaStream_t stream);
+
+    // Register-sliding FP32 kernel (amb_step_f32.cu). Returns cudaErrorNotSupported
+    // when the grid shape is outside its fast-path constraints.
+    cudaError_t launch_step_f32_sliding(const float* phi_in, float* phi_out, __nv_bfloat16* comp, int comp_mode,
+                                        const StepParams& p, int noise_mode, const float* injected, int variant,
+                                        cudaStream_t stream);
+    bool step_f32_sliding_supported(int ny, int nx, int variant);
+
+    template <typename Real>
+    cudaError_t launch_terms(const Real* phi, double* out, const StepParams& p, int noise_mode, const Real* injected,
+                             cudaStream_t stream);
+
+    int mass_partials(size_t n);
+    template <typename Real>
+    cudaError_t launch_mass(const Real* f, size_t n, double* out, double* scratch, int nparts, cudaStream_t stream);
+
+    template <typename Real>
+    cudaError_t launch_nonfinite(const Real* f, size_t n, int* flag, cudaStream_t stream);
+
+    cudaError_t launch_convert_f64_to_f32(const double* src, float* dst, size_t n, cudaStream_t stream);
+    cudaError_t launch_convert_f32_to_f64(const float* src, double* dst, size_t n, cudaStream_t stream);
+}

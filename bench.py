@@ -1,0 +1,370 @@
+#!/usr/bin/env python3
+"""Throughput benchmark of the Active Model B+ step on GB300.
+
+Metric: Gsite-updates/s of the explicit-Euler AMB+ step at 4096^2 (and its
+fraction of the HBM roofline at 8 B per site-update).
+
+Workload (synthetic, seeded): 4096 x 4096 periodic, dt=1e-3, dx=dy=1,
+a=-0.25 b=0 c=0.25 kappa=1 zeta=-1 lambda=0.5 T=0.05, phi = -0.4 + 0.01 N(0,1)
+(numpy seed 2024), Philox noise, FP32 field with bf16 Kahan residual (f32c).
+One bench step = one ``Integrator.run(inner)`` call (``inner`` Euler steps,
+default 100) on device-resident buffers; the L2 is flushed (256 MiB write)
+before every timed step.
+
+Keys beyond the base contract:
+  e2e          same metric through the C handle (amb_integrator_*) with pinned
+               float64 host buffers: set_field + run(inner) + get_field per step.
+  roofline     step kernel: 8 B x sites per launch / CUDA-event launch time,
+               against MEASURED_PEAKS.json hbm_gbs.
+  cpu_baseline the oracle port (C, OpenMP) on the host cores, bounded sample.
+  clocks       nvidia-smi samples during the timed region.
+
+``--impl reference`` times the reference's CPU implementation of the step
+(oracle/_ref where it loads, else the oracle port) on all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "active-model-bplus_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Gsite-updates/s 4096^2 (%HBM peak); surrogate vs plain time-to-t at S(k) tol"
+UNIT = "Gsite-updates/s"
+BYTES_PER_SITE = 8  # algorithmic: read phi (4 B) + write phi (4 B), FP32 path
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--size", type=int, default=4096)
+    ap.add_argument("--inner", type=int, default=100)
+    ap.add_argument("--precision", choices=["f32c", "f32", "f64"], default="f32c")
+    ap.add_argument("--kernel", choices=["auto", "tile", "sliding"], default="auto")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--temperature", type=float, default=0.05)
+    return ap.parse_args()
+
+
+def workload(args):
+    return dict(ny=args.size, nx=args.size, dt=1e-3, dx=1.0, dy=1.0, a=-0.25, b=0.0, c=0.25, kappa=1.0,
+                lamb=0.5, zeta=-1.0, T=args.temperature, phi0=-0.4, amp=0.01, seed=2024)
+
+
+def initial_field(w, rank=0):
+    rng = np.random.default_rng(w["seed"] + rank)
+    return w["phi0"] + w["amp"] * rng.standard_normal((w["ny"], w["nx"]))
+
+
+def config_of(args, w):
+    return {
+        "workload": f"AMB+ {w['ny']}x{w['nx']} periodic, dt=1e-3, a=-0.25 b=0 c=0.25 kappa=1 zeta=-1 lambda=0.5 "
+                    f"T={w['T']}, phi0=-0.4+0.01N(0,1), Philox noise",
+        "ny": w["ny"], "nx": w["nx"], "precision": args.precision, "kernel": args.kernel,
+        "inner_steps": args.inner, "l2": "flushed before every timed step (256 MiB write)",
+        "parallelism": f"replicas{args.gpus}",
+    }
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        if not self.lines:
+            return None
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ helpers
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def measured_traffic(args):
+    """Per-launch DRAM bytes of the step kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "step_kernel_traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    key = f"{args.precision}_{args.size}"
+    return d.get(key)
+
+
+def cpu_baseline(w, seconds: float = 10.0, use_reference: bool = True):
+    """Time the CPU implementation of the same step on the host cores (bounded sample)."""
+    import oracle
+    field = initial_field(w)
+    threads = os.cpu_count() or 1
+    ref = oracle.reference_lib(fast=True) if use_reference else None
+    p = oracle.Params(dt=w["dt"], dx=w["dx"], dy=w["dy"], a=w["a"], b=w["b"], c=w["c"], kappa=w["kappa"],
+                      lamb=w["lamb"], zeta=w["zeta"], T=w["T"])
+    if ref is not None and w["b"] == 0 and w["a"] == -w["c"]:
+        kind, cores = "reference", 1
+
+        def run(n):
+            return oracle.tjhung_run(field, n, w["dt"], w["dx"], w["c"], w["kappa"], w["lamb"], w["zeta"], fast=True)
+        desc = "test/tjhung_ambplus.h (-Ofast, serial; noise off: its drand48 noise cannot be keyed)"
+    else:
+        kind, cores = "port", threads
+
+        def run(n):
+            return oracle.run(field, p, n, noise="philox" if w["T"] else "none", seed=1, nthreads=threads)
+        desc = "oracle/amb_oracle.c (OpenMP) with Philox noise"
+    t0 = time.perf_counter()
+    run(1)
+    t1 = time.perf_counter() - t0
+    nsteps = int(max(1, min(200, round(seconds / max(t1, 1e-6)))))
+    t0 = time.perf_counter()
+    run(nsteps)
+    dt = time.perf_counter() - t0
+    sites = w["ny"] * w["nx"]
+    return {"value": nsteps * sites / dt / 1e9, "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": f"{nsteps} Euler steps of the {w['ny']}x{w['nx']} workload ({dt:.1f} s); {desc}"}
+
+
+# ------------------------------------------------------------------ arms
+
+def run_reference_arm(args, w, rank, world):
+    if rank != 0:
+        return
+    import oracle
+    field = initial_field(w)
+    threads = os.cpu_count() or 1
+    p = oracle.Params(dt=w["dt"], dx=w["dx"], dy=w["dy"], a=w["a"], b=w["b"], c=w["c"], kappa=w["kappa"],
+                      lamb=w["lamb"], zeta=w["zeta"], T=w["T"])
+    ref = oracle.reference_lib(fast=True)
+    if ref is not None:
+        kind, cores, desc = "reference", 1, "test/tjhung_ambplus.h -Ofast serial, noise off"
+
+        def step():
+            oracle.tjhung_run(field, 1, w["dt"], w["dx"], w["c"], w["kappa"], w["lamb"], w["zeta"], fast=True)
+    else:
+        kind, cores, desc = "port", threads, "oracle/amb_oracle.c, OpenMP, Philox noise"
+
+        def step():
+            oracle.run(field, p, 1, noise="philox" if w["T"] else "none", seed=1, nthreads=threads)
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    sites = w["ny"] * w["nx"]
+    value = args.steps * sites / dt / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": dict(config_of(args, w), inner_steps=1, precision="f64 (CPU)"),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": f"each step = 1 Euler step of the {w['ny']}x{w['nx']} workload; {desc}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, w, rank, world, dist):
+    import torch
+    from activemodelbplus.integrator import Integrator, Model, Stencil, _native as N
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stencil = Stencil(w["dt"], w["dx"], w["dy"])
+    model = Model(w["a"], w["b"], w["c"], w["kappa"], w["lamb"], w["zeta"], w["T"])
+    field = initial_field(w, rank)
+    sites = w["ny"] * w["nx"]
+    sim = Integrator(field, stencil, model, precision=args.precision, seed=1000 + rank, kernel=args.kernel)
+    flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        sim.run(args.inner)
+    barrier()
+
+    step_ms, kern_ms = [], []
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    with ClockSampler(dev.index) as clocks:
+        barrier()
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            ev[0].record()
+            sim._events = (ev[1], ev[2])
+            sim.run(args.inner)
+            ev[3].record()
+            ev[3].synchronize()
+            step_ms.append(ev[0].elapsed_time(ev[3]))
+            kern_ms.append(ev[1].elapsed_time(ev[2]))
+        sim._events = None
+        barrier()
+    total_ms = sum(step_ms)
+    launch_ms = sum(kern_ms) / (args.steps * args.inner)
+    if dist is not None:
+        t = torch.tensor([total_ms, launch_ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, launch_ms = float(t[0]), float(t[1])
+    value = world * args.steps * args.inner * sites / (total_ms / 1e3) / 1e9
+
+    # e2e through the C handle with pinned float64 host buffers
+    e2e = None
+    if not args.no_e2e:
+        L = N.lib()
+        prec = {"f64": N.AMB_F64, "f32": N.AMB_F32, "f32c": N.AMB_F32C}[args.precision]
+        host_in = torch.from_numpy(field).pin_memory()
+        host_out = torch.empty_like(host_in).pin_memory()
+        h = ctypes.c_void_p()
+        s, m = N.stencil_struct(stencil), N.model_struct(model)
+        rc = L.amb_integrator_create(host_in.data_ptr(), w["ny"], w["nx"], ctypes.byref(s), ctypes.byref(m), prec,
+                                     2000 + rank, ctypes.byref(h))
+        if rc:
+            raise RuntimeError(N.last_error())
+        try:
+            def e2e_step():
+                for rc in (L.amb_integrator_set_field(h, host_in.data_ptr()), L.amb_integrator_run(h, args.inner),
+                           L.amb_integrator_get_field(h, host_out.data_ptr())):
+                    if rc:
+                        raise RuntimeError(N.last_error())
+            for _ in range(args.warmup):
+                e2e_step()
+            barrier()
+            wall = 0.0
+            for k in range(args.steps):
+                flush.fill_(float(k))
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                e2e_step()
+                wall += time.perf_counter() - t0
+            if dist is not None:
+                t = torch.tensor([wall], dtype=torch.float64, device=dev)
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                wall = float(t[0])
+            e2e = {"value": world * args.steps * args.inner * sites / wall / 1e9, "unit": UNIT,
+                   "h2d_bytes_per_step": int(host_in.numel() * 8), "d2h_bytes_per_step": int(host_out.numel() * 8)}
+        finally:
+            L.amb_integrator_destroy(h)
+
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    bytes_per_site = BYTES_PER_SITE if args.precision != "f64" else 16
+    achieved = bytes_per_site * sites / (launch_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "f64" else "f32", "data": "synthetic", "config": config_of(args, w),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                     else "fallback 6.8 TB/s", "traffic": measured_traffic(args),
+                     "kernel": "AMB+ fused step", "launch_us": launch_ms * 1e3,
+                     "algorithmic_bytes_per_launch": bytes_per_site * sites},
+        "e2e": e2e,
+        "gpu_launches": args.steps * (args.inner + 1),
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu and world == 1:
+        line["cpu_baseline"] = cpu_baseline(w)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    w = workload(args)
+    if args.impl == "reference":
+        return run_reference_arm(args, w, rank, world)
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        tdist.init_process_group("nccl")
+        dist = tdist
+    try:
+        run_ours(args, w, rank, world, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

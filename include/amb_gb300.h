@@ -1,0 +1,170 @@
+/*
+ * amb_gb300.h — C ABI of the GB300-native Active Model B+ integrator.
+ *
+ * Drop-in boundary for the reference's plain integrator (tranqui/active-model-bplus).
+ * The reference exposes its integrator to Python through a pybind11 module
+ * (src/integrator.cc:31-123) over the C++ class Integrator
+ * (src/integrator.h:24-81, src/integrator.cu:288-538). This header replaces that
+ * boundary with plain C: opaque handles, plain pointers and sizes, int status.
+ *
+ * Two layers:
+ *   1. amb_integrator_*  — the reference's Integrator class, one call per method,
+ *                          host buffers in and out (what a cgo / JNI / ctypes
+ *                          binding of the reference's class would bind).
+ *   2. amb_step_*, amb_terms_*, amb_mass_*, amb_check_finite_* — stateless,
+ *                          stream-ordered calls on caller-owned DEVICE buffers
+ *                          (what the Python host layer drives with torch tensors).
+ *
+ * Conventions
+ *   - Fields are row-major (nrows, ncols), index = col + row * ncols, axis 0 = y
+ *     (src/integrator.cu:59, src/integrator.cc:108-109). Periodic in both axes.
+ *     Any nrows, ncols >= 1 is accepted (the reference needs multiples of 8).
+ *   - Every call returns AMB_OK (0) or an AMB_ERR_* code; amb_last_error() gives
+ *     the calling thread's message for the last failing call. Calls never throw.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).
+ *   - Parameters travel with each call or handle: there is no process-global
+ *     state (the reference keeps them in __constant__ memory, src/parameters.cu:6-8),
+ *     so independent integrators may run concurrently on different streams.
+ */
+#ifndef AMB_GB300_H
+#define AMB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+#define AMB_OK 0
+#define AMB_ERR_INVALID 1     /* bad argument: size, pointer, precision, kernel id */
+#define AMB_ERR_CUDA 2        /* CUDA runtime error (reference: kernel::throw_errors, src/integrator.cu:21-30) */
+#define AMB_ERR_NONFINITE 3   /* field became NaN/Inf (reference: src/integrator.cu:524-537) */
+#define AMB_ERR_NOMEM 4       /* device or host allocation failed */
+#define AMB_ERR_UNSUPPORTED 5 /* valid request the chosen kernel cannot serve */
+
+/* --------------------------------------------------------------- parameters */
+/* HostStencilParams (src/parameters.h:23-41). */
+typedef struct amb_stencil
+{
+    double dt, dx, dy;
+} amb_stencil;
+
+/* ActiveModelBPlusParams (src/parameters.h:54-77): mu = a phi + b phi^2 + c phi^3 - kappa lap phi,
+ * active terms lambda |grad phi|^2 and zeta (lap phi) grad phi, noise temperature T. */
+typedef struct amb_model
+{
+    double a, b, c, kappa, lambda, zeta, temperature;
+} amb_model;
+
+/* Storage precisions. The reference has FP64 only (src/math_primitives.h:5). */
+#define AMB_F64 0  /* double field; parity path */
+#define AMB_F32 1  /* float field, float arithmetic */
+#define AMB_F32C 2 /* float field + 16-bit (bf16) Kahan residual plane: compensated update */
+
+/* Selectors for the current / chemical-potential getters (src/integrator.h:41-51). */
+#define AMB_CURRENT_TOTAL 0         /* get_current */
+#define AMB_CURRENT_DETERMINISTIC 1 /* get_deterministic_current */
+#define AMB_CURRENT_PASSIVE 2       /* get_passive_current */
+#define AMB_CURRENT_ACTIVE 3        /* get_active_current */
+#define AMB_CURRENT_LAMBDA 4        /* get_lambda_current */
+#define AMB_CURRENT_CIRCULATING 5   /* get_circulating_current */
+#define AMB_CURRENT_RANDOM 6        /* get_random_current */
+#define AMB_MU_TOTAL 0              /* get_chemical_potential */
+#define AMB_MU_PASSIVE 1            /* get_passive_chemical_potential */
+#define AMB_MU_ACTIVE 2             /* get_active_chemical_potential */
+
+/* Kernel selectors for amb_step_f32 (AMB_KERNEL_AUTO picks the fastest valid one). */
+#define AMB_KERNEL_AUTO 0
+#define AMB_KERNEL_TILE 1    /* shared-memory tile kernel, any grid */
+#define AMB_KERNEL_SLIDING 2 /* register-sliding FP32 kernel (needs ncols % 4 == 0) */
+
+/* Number of FP64 planes written by amb_terms_*: mu_p, mu_a, J_p(y,x), J_l(y,x), J_c(y,x), J_r(y,x). */
+#define AMB_NTERMS 10
+
+const char* amb_version(void);
+/* Message of the calling thread's last failing call ("" if none). Replaces the
+ * reference's CudaError what() string (src/integrator.h:10-14). */
+const char* amb_last_error(void);
+
+/* ====================================================== layer 1: Integrator */
+typedef struct amb_integrator amb_integrator;
+
+/* Integrator::Integrator(field, stencil, model) (src/integrator.cu:288-333).
+ * host_field: nrows*ncols doubles. precision: AMB_F64 / AMB_F32 / AMB_F32C.
+ * seed keys the Philox noise (the reference draws a non-deterministic curand seed,
+ * src/integrator.cu:320-323); the same seed reproduces a run exactly. */
+int amb_integrator_create(const double* host_field, int nrows, int ncols, const amb_stencil* stencil,
+                          const amb_model* model, int precision, uint64_t seed, amb_integrator** out);
+/* Integrator::~Integrator (src/integrator.cu:353-366). NULL is ignored. */
+void amb_integrator_destroy(amb_integrator* h);
+/* Integrator::run(nsteps) (src/integrator.cu:497-538): advances nsteps steps, blocks until
+ * done, then checks the field is finite (AMB_ERR_NONFINITE otherwise). As in the
+ * reference, the timestep counter advances by nsteps even when nsteps <= 0. */
+int amb_integrator_run(amb_integrator* h, int nsteps);
+/* Integrator::get_field (src/integrator.cu:378-383): copies the field out as doubles. */
+int amb_integrator_get_field(amb_integrator* h, double* host_out);
+/* No reference counterpart: replace the field (resume from a checkpoint); residual cleared. */
+int amb_integrator_set_field(amb_integrator* h, const double* host_field);
+/* get_chemical_potential / get_passive_... / get_active_... (src/integrator.cu:385-404). */
+int amb_integrator_get_chemical_potential(amb_integrator* h, int which, double* host_out);
+/* get_current and friends (src/integrator.cu:406-465): two planes (y then x component). */
+int amb_integrator_get_current(amb_integrator* h, int which, double* host_y, double* host_x);
+/* get_timestep / get_time (src/integrator.h:53-61). */
+int amb_integrator_get_timestep(const amb_integrator* h, int64_t* out);
+int amb_integrator_get_time(const amb_integrator* h, double* out);
+/* No reference counterpart: jump the step counter (exact resume of (field, step, seed)). */
+int amb_integrator_set_timestep(amb_integrator* h, int64_t timestep);
+/* get_stencil / get_model (src/integrator.cu:368-376). */
+int amb_integrator_get_stencil(const amb_integrator* h, amb_stencil* out);
+int amb_integrator_get_model(const amb_integrator* h, amb_model* out);
+int amb_integrator_get_shape(const amb_integrator* h, int* nrows, int* ncols, int* precision);
+
+/* ============================================ layer 2: device-pointer calls */
+
+/* nsteps fused explicit-Euler steps on a device field (the reference's run loop,
+ * src/integrator.cu:507-518, whose three kernels per step become one launch).
+ * field and spare are two device buffers of nrows*ncols elements; the steps
+ * ping-pong between them, and *result_in_spare (if not NULL) is set to 1 when the
+ * result ended in `spare`, 0 when in `field`.
+ * The update from step s to s+1 uses currents at step s with noise keyed on
+ * (seed, s): steps run from step0 to step0 + nsteps.
+ * injected_noise: NULL for Philox noise (or none when temperature == 0); otherwise
+ * nsteps * 2 * nrows * ncols standard normals, per step the y plane then the x plane
+ * (J_r = sqrt(2T/(dt dx dy)) * xi, src/integrator.cu:106-109).
+ * Asynchronous on `stream`. */
+int amb_step_f64(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows, int ncols,
+                 double* field, double* spare, int64_t step0, int nsteps, const double* injected_noise,
+                 void* stream, int* result_in_spare);
+/* FP32 storage. residual: NULL for plain FP32 (AMB_F32), else a device plane of
+ * nrows*ncols bf16 words updated in place (AMB_F32C; zero it before the first step).
+ * kernel: AMB_KERNEL_*. */
+int amb_step_f32(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows, int ncols,
+                 float* field, float* spare, uint16_t* residual, int64_t step0, int nsteps,
+                 const float* injected_noise, int kernel, void* stream, int* result_in_spare);
+
+/* Every term of the reference's forces/currents kernels (src/integrator.cu:46-176) at
+ * timestep `step`, as AMB_NTERMS FP64 device planes in `out` (order in AMB_NTERMS).
+ * injected_noise: NULL (Philox) or 2 planes (y, x) of standard normals. */
+int amb_terms_f64(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows, int ncols,
+                  const double* field, int64_t step, const double* injected_noise, double* out, void* stream);
+int amb_terms_f32(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows, int ncols,
+                  const float* field, int64_t step, const float* injected_noise, double* out, void* stream);
+
+/* FP64 compensated sum of a device field into out_sum (one double, device memory).
+ * scratch: device memory of at least amb_mass_scratch_bytes(n) bytes. */
+size_t amb_mass_scratch_bytes(int64_t n);
+int amb_mass_f64(const double* field, int64_t n, double* out_sum, void* scratch, size_t scratch_bytes, void* stream);
+int amb_mass_f32(const float* field, int64_t n, double* out_sum, void* scratch, size_t scratch_bytes, void* stream);
+
+/* ORs 1 into *flag (device int) when any element of the field is NaN or Inf
+ * (src/integrator.cu:265-272). The caller zeroes the flag. */
+int amb_check_finite_f64(const double* field, int64_t n, int* flag, void* stream);
+int amb_check_finite_f32(const float* field, int64_t n, int* flag, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AMB_GB300_H */
