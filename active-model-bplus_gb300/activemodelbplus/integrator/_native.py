@@ -34,6 +34,11 @@ class amb_model(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in ("a", "b", "c", "kappa", "lamb", "zeta", "temperature")]
 
 
+class amb_kernel_config(ctypes.Structure):
+    _fields_ = [("kernel", ctypes.c_int), ("seg_rows", ctypes.c_int), ("pairs_per_cta", ctypes.c_int),
+                ("reserved", ctypes.c_int)]
+
+
 _VP = ctypes.c_void_p
 _I = ctypes.c_int
 _I64 = ctypes.c_int64
@@ -61,6 +66,8 @@ SIGNATURES = {
     "amb_integrator_get_shape": (_I, [_VP, _IP, _IP, _IP]),
     "amb_step_f64": (_I, [_SP, _MP, _U64, _I, _I, _VP, _VP, _I64, _I, _VP, _VP, _IP]),
     "amb_step_f32": (_I, [_SP, _MP, _U64, _I, _I, _VP, _VP, _VP, _I64, _I, _VP, _I, _VP, _IP]),
+    "amb_step_f32_ex": (_I, [_SP, _MP, _U64, _I, _I, _VP, _VP, _VP, _I64, _I, _VP, ctypes.POINTER(amb_kernel_config),
+                             _VP, _IP]),
     "amb_terms_f64": (_I, [_SP, _MP, _U64, _I, _I, _VP, _I64, _VP, _VP, _VP]),
     "amb_terms_f32": (_I, [_SP, _MP, _U64, _I, _I, _VP, _I64, _VP, _VP, _VP]),
     "amb_mass_scratch_bytes": (ctypes.c_size_t, [_I64]),

@@ -106,41 +106,65 @@ extern "C" int amb_step_f64(const amb_stencil* stencil, const amb_model* model, 
     return AMB_OK;
 }
 
-extern "C" int amb_step_f32(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows, int ncols,
-                            float* field, float* spare, uint16_t* residual, int64_t step0, int nsteps,
-                            const float* injected_noise, int kernel, void* stream, int* result_in_spare)
+namespace
+{
+    bool aligned(const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
+}
+
+extern "C" int amb_step_f32_ex(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows,
+                               int ncols, float* field, float* spare, uint16_t* residual, int64_t step0, int nsteps,
+                               const float* injected_noise, const amb_kernel_config* config, void* stream,
+                               int* result_in_spare)
 {
     if (int rc = check_shape(nrows, ncols)) return rc;
     if (int rc = check_params(stencil, model)) return rc;
     if (!field || !spare || field == spare) return fail(AMB_ERR_INVALID, "field and spare must be distinct device buffers");
     if (nsteps < 0) return fail(AMB_ERR_INVALID, "nsteps must be >= 0");
-    if (kernel < AMB_KERNEL_AUTO || kernel > AMB_KERNEL_SLIDING) return fail(AMB_ERR_INVALID, "unknown kernel selector");
+    amb_kernel_config cfg{AMB_KERNEL_AUTO, 0, 0, 0};
+    if (config) cfg = *config;
+    if (cfg.kernel < AMB_KERNEL_AUTO || cfg.kernel > AMB_KERNEL_SLIDING) return fail(AMB_ERR_INVALID, "unknown kernel selector");
+    if (cfg.seg_rows < 0 || cfg.pairs_per_cta < 0 || cfg.pairs_per_cta > 4 || cfg.pairs_per_cta == 3)
+        return fail(AMB_ERR_INVALID, "kernel config: seg_rows >= 0, pairs_per_cta in {0, 1, 2, 4}");
     const size_t n = size_t(nrows) * ncols;
     const int mode = noise_mode_for(model, injected_noise);
     const int comp = residual ? amb::COMP_BF16 : amb::COMP_NONE;
     auto* res = reinterpret_cast<__nv_bfloat16*>(residual);
+    const bool fits = amb::step_f32_sliding_supported(nrows, ncols, 0) && aligned(field, 16) && aligned(spare, 16)
+                      && (!residual || aligned(residual, 8)) && (!injected_noise || aligned(injected_noise, 16));
     bool sliding = false;
-    if (kernel == AMB_KERNEL_SLIDING)
+    if (cfg.kernel == AMB_KERNEL_SLIDING)
     {
-        if (!amb::step_f32_sliding_supported(nrows, ncols, 0))
-            return fail(AMB_ERR_UNSUPPORTED, "sliding kernel needs ncols % 4 == 0 and nrows, ncols >= 16");
+        if (!fits)
+            return fail(AMB_ERR_UNSUPPORTED, "sliding kernel needs ncols % 4 == 0, ncols >= 136 and 16-byte aligned "
+                                             "field buffers (8-byte residual)");
         sliding = true;
     }
-    else if (kernel == AMB_KERNEL_AUTO)
-        sliding = amb::step_f32_sliding_supported(nrows, ncols, 0);
+    else if (cfg.kernel == AMB_KERNEL_AUTO)
+        sliding = fits;
+    const int pairs_code = cfg.pairs_per_cta == 1 ? 1 : cfg.pairs_per_cta == 4 ? 3 : cfg.pairs_per_cta == 2 ? 2 : 0;
+    const int variant = (cfg.seg_rows << 4) | pairs_code;
     float* cur = field;
     float* nxt = spare;
     for (int s = 0; s < nsteps; ++s)
     {
         amb::StepParams p = make_params(stencil, model, seed, nrows, ncols, step0 + s);
         const float* inj = injected_noise ? injected_noise + size_t(s) * 2 * n : nullptr;
-        cudaError_t e = sliding ? amb::launch_step_f32_sliding(cur, nxt, res, comp, p, mode, inj, 0, as_stream(stream))
+        cudaError_t e = sliding ? amb::launch_step_f32_sliding(cur, nxt, res, comp, p, mode, inj, variant, as_stream(stream))
                                 : amb::launch_step_tile<float>(cur, nxt, res, comp, p, mode, inj, as_stream(stream));
         if (e != cudaSuccess) return cuda_fail(e, "amb_step_f32");
         std::swap(cur, nxt);
     }
     if (result_in_spare) *result_in_spare = (cur == spare) ? 1 : 0;
     return AMB_OK;
+}
+
+extern "C" int amb_step_f32(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows, int ncols,
+                            float* field, float* spare, uint16_t* residual, int64_t step0, int nsteps,
+                            const float* injected_noise, int kernel, void* stream, int* result_in_spare)
+{
+    amb_kernel_config cfg{kernel, 0, 0, 0};
+    return amb_step_f32_ex(stencil, model, seed, nrows, ncols, field, spare, residual, step0, nsteps, injected_noise,
+                           &cfg, stream, result_in_spare);
 }
 
 // ------------------------------------------------------------------ terms

@@ -37,10 +37,16 @@ namespace amb
         return k == 1 ? 4.0 / 5 : k == 2 ? -1.0 / 5 : k == 3 ? 4.0 / 105 : -1.0 / 280;
     }
 
-    __host__ __device__ inline int wrap_index(long long i, int n)
+    // Periodic index in [0, n). The common cases (already inside, or one period
+    // out) take no division; only grids smaller than the stencil reach the
+    // general remainder. |i| < 2^31 for every caller (n < 2^30).
+    __host__ __device__ __forceinline__ int wrap_index(int i, int n)
     {
-        long long r = i % n;
-        return int(r < 0 ? r + n : r);
+        if ((unsigned)i < (unsigned)n) return i;
+        if (i < 0 && i >= -n) return i + n;
+        if (i >= n && i - n < n) return i - n;
+        int r = i % n;
+        return r < 0 ? r + n : r;
     }
 
     // ------------------------------------------------------------ Philox noise
@@ -61,6 +67,21 @@ namespace amb
             c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
             k0 += W0;
             k1 += W1;
+        }
+        return c;
+    }
+
+    // Philox4x32-10 with the ten round keys precomputed (rk0[i] = k0 + i W0,
+    // rk1[i] = k1 + i W1): same output as philox4x32_10, no key arithmetic per call.
+    __device__ __forceinline__ U4 philox4x32_10_rk(U4 c, const uint32_t (&rk0)[10], const uint32_t (&rk1)[10])
+    {
+        constexpr uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+#pragma unroll
+        for (int round = 0; round < 10; ++round)
+        {
+            uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+            uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+            c = U4{hi1 ^ c.y ^ rk0[round], lo1, hi0 ^ c.w ^ rk1[round], lo0};
         }
         return c;
     }

@@ -19,6 +19,7 @@ namespace amb
                                         const StepParams& p, int noise_mode, const float* injected, int variant,
                                         cudaStream_t stream);
     bool step_f32_sliding_supported(int ny, int nx, int variant);
+    int sliding_default_seg_h(int ny, int nx);
 
     template <typename Real>
     cudaError_t launch_terms(const Real* phi, double* out, const StepParams& p, int noise_mode, const Real* injected,

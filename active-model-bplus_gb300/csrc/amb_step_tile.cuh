@@ -146,8 +146,8 @@ namespace amb
         for (int e = tid; e < G::LY * G::LX; e += nthr)
         {
             int i = e / G::LX, j = e - i * G::LX;
-            int gr = wrap_index((long long)r0 + i - G::H, ny);
-            int gc = wrap_index((long long)c0 + j - G::H, nx);
+            int gr = wrap_index(r0 + i - G::H, ny);
+            int gc = wrap_index(c0 + j - G::H, nx);
             PHI[e] = phi_in[(size_t)gr * nx + gc];
         }
         __syncthreads();
@@ -185,7 +185,7 @@ namespace amb
             Real xi = 0;
             if (noise_mode != NOISE_OFF)
             {
-                int gr = wrap_index((long long)r0 + i, ny), gc = wrap_index((long long)c0 + j, nx);
+                int gr = wrap_index(r0 + i, ny), gc = wrap_index(c0 + j, nx);
                 xi = noise_mode == NOISE_PHILOX ? noise_normal<Real>(p.seed, p.step, gr, gc, 0)
                                                 : injected[(size_t)gr * nx + gc];
             }
@@ -197,7 +197,7 @@ namespace amb
             Real xi = 0;
             if (noise_mode != NOISE_OFF)
             {
-                int gr = wrap_index((long long)r0 + i, ny), gc = wrap_index((long long)c0 + j, nx);
+                int gr = wrap_index(r0 + i, ny), gc = wrap_index(c0 + j, nx);
                 xi = noise_mode == NOISE_PHILOX ? noise_normal<Real>(p.seed, p.step, gr, gc, 1)
                                                 : injected[plane + (size_t)gr * nx + gc];
             }

@@ -78,7 +78,17 @@ typedef struct amb_model
 /* Kernel selectors for amb_step_f32 (AMB_KERNEL_AUTO picks the fastest valid one). */
 #define AMB_KERNEL_AUTO 0
 #define AMB_KERNEL_TILE 1    /* shared-memory tile kernel, any grid */
-#define AMB_KERNEL_SLIDING 2 /* register-sliding FP32 kernel (needs ncols % 4 == 0) */
+#define AMB_KERNEL_SLIDING 2 /* warp-pair sliding FP32 kernel (ncols % 4 == 0, ncols >= 136, 16-byte aligned) */
+
+/* Explicit kernel configuration for amb_step_f32_ex (zeros mean defaults).
+ * seg_rows: rows per warp-pair task of the sliding kernel; pairs_per_cta: 1, 2 or 4. */
+typedef struct amb_kernel_config
+{
+    int kernel;
+    int seg_rows;
+    int pairs_per_cta;
+    int reserved;
+} amb_kernel_config;
 
 /* Number of FP64 planes written by amb_terms_*: mu_p, mu_a, J_p(y,x), J_l(y,x), J_c(y,x), J_r(y,x). */
 #define AMB_NTERMS 10
@@ -143,6 +153,12 @@ int amb_step_f64(const amb_stencil* stencil, const amb_model* model, uint64_t se
 int amb_step_f32(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows, int ncols,
                  float* field, float* spare, uint16_t* residual, int64_t step0, int nsteps,
                  const float* injected_noise, int kernel, void* stream, int* result_in_spare);
+
+/* amb_step_f32 with an explicit kernel configuration (NULL = defaults). */
+int amb_step_f32_ex(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows, int ncols,
+                    float* field, float* spare, uint16_t* residual, int64_t step0, int nsteps,
+                    const float* injected_noise, const amb_kernel_config* config, void* stream,
+                    int* result_in_spare);
 
 /* Every term of the reference's forces/currents kernels (src/integrator.cu:46-176) at
  * timestep `step`, as AMB_NTERMS FP64 device planes in `out` (order in AMB_NTERMS).

@@ -1,0 +1,131 @@
+"""The FP32 kernels against each other and against the oracle, through the
+device-pointer C ABI (amb_step_f32_ex).
+
+Covers the warp-pair sliding kernel's decomposition (row segments, strips, the
+overlapping last strip, periodic wrap of the row window), its Philox and
+injected noise, and both FP32 storage modes. Tolerances are stated per test:
+the two FP32 kernels evaluate the same operators in a different rounding
+order, so they agree to FP32 rounding, not bitwise; one kernel under different
+decompositions agrees bitwise.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import Params
+
+pytestmark = pytest.mark.gpu
+
+
+def native():
+    from activemodelbplus.integrator import _native as N
+    return N
+
+
+def run_f32(field, p: Params, nsteps, *, kernel=1, seg_rows=0, pairs=0, comp=True, seed=7, injected=None, step0=0):
+    import torch
+    N = native()
+    ny, nx = field.shape
+    a = torch.from_numpy(field.astype(np.float32)).cuda()
+    b = torch.empty_like(a)
+    res = torch.zeros((ny, nx), dtype=torch.int16, device="cuda") if comp else None
+    inj = None if injected is None else torch.from_numpy(injected.astype(np.float32)).cuda()
+    s = N.amb_stencil(p.dt, p.dx, p.dy)
+    m = N.amb_model(p.a, p.b, p.c, p.kappa, p.lamb, p.zeta, p.T)
+    cfg = N.amb_kernel_config(kernel, seg_rows, pairs, 0)
+    flag = ctypes.c_int(0)
+    rc = N.lib().amb_step_f32_ex(ctypes.byref(s), ctypes.byref(m), seed, ny, nx, a.data_ptr(), b.data_ptr(),
+                                 res.data_ptr() if comp else None, step0, nsteps,
+                                 inj.data_ptr() if inj is not None else None, ctypes.byref(cfg),
+                                 torch.cuda.current_stream().cuda_stream, ctypes.byref(flag))
+    assert rc == 0, N.last_error()
+    out = (b if flag.value else a).cpu().numpy().astype(np.float64)
+    torch.cuda.synchronize()
+    return out
+
+
+AMB = dict(dt=1e-3, dx=1.0, dy=1.0, a=-0.25, b=0.0, c=0.25, kappa=1.0, lamb=0.5, zeta=-1.0)
+
+
+def initial(shape, seed=0):
+    rng = np.random.default_rng(seed)
+    return -0.4 + 0.05 * rng.standard_normal(shape)
+
+
+@pytest.mark.parametrize("shape", [(256, 256), (200, 140), (37, 340), (17, 256), (96, 448), (5, 136)])
+@pytest.mark.parametrize("T", [0.0, 0.05])
+def test_sliding_matches_tile(shape, T):
+    """Both FP32 kernels, 30 steps, plain FP32 and compensated: max |diff| < 2e-6
+    (different rounding order of the same operators; fields ~0.4)."""
+    field = initial(shape, seed=shape[0])
+    p = Params(T=T, **AMB)
+    for comp in (False, True):
+        tile = run_f32(field, p, 30, kernel=1, comp=comp)
+        slid = run_f32(field, p, 30, kernel=2, comp=comp)
+        assert np.isfinite(slid).all()
+        assert np.abs(tile - slid).max() < 2e-6, (comp, np.abs(tile - slid).max())
+
+
+@pytest.mark.parametrize("seg_rows,pairs", [(0, 0), (16, 1), (37, 2), (100, 4), (1000, 2), (1, 1)])
+def test_sliding_decomposition_is_exact(seg_rows, pairs):
+    """Results do not depend on how rows are split into segments or warp pairs into CTAs
+    (per-site arithmetic and Philox keys are decomposition independent): bitwise."""
+    field = initial((144, 560), seed=3)
+    p = Params(T=0.05, **AMB)
+    ref = run_f32(field, p, 12, kernel=2, seg_rows=64, pairs=2)
+    got = run_f32(field, p, 12, kernel=2, seg_rows=seg_rows, pairs=pairs)
+    assert np.array_equal(ref, got)
+
+
+@pytest.mark.parametrize("comp,tol", [(True, 2e-6), (False, 2e-5)])
+def test_sliding_tracks_fp64_oracle(comp, tol):
+    """AMB+ with Philox noise, 128 x 256, 100 steps: FP32 kernel vs the FP64 oracle with the
+    same noise definition. Bounds from the FP32 rounding of field and normals."""
+    field = initial((128, 256), seed=5)
+    p = Params(T=0.05, **AMB)
+    got = run_f32(field, p, 100, kernel=2, comp=comp, seed=11)
+    ref = oracle.run(field, p, 100, noise="philox", seed=11, nthreads=4)
+    assert np.abs(got - ref).max() < tol
+
+
+def test_sliding_injected_noise():
+    """Host-injected normals, 5 steps, FP32 compensated vs the FP64 oracle: < 1e-6."""
+    rng = np.random.default_rng(8)
+    field = initial((64, 272), seed=8)
+    noise = rng.standard_normal((5, 2, 64, 272))
+    p = Params(T=0.05, **AMB)
+    got = run_f32(field, p, 5, kernel=2, comp=True, injected=noise)
+    ref = oracle.run(field, p, 5, noise="injected", injected=noise.astype(np.float32).astype(np.float64))
+    assert np.abs(got - ref).max() < 1e-6
+
+
+def test_sliding_step_offset_and_chunking():
+    """Running 20 steps as 7 + 13 (step0 carries the Philox key) equals 20 at once."""
+    import torch
+    field = initial((80, 224), seed=9)
+    p = Params(T=0.05, **AMB)
+    whole = run_f32(field, p, 20, kernel=2, comp=False)
+    part = run_f32(field, p, 7, kernel=2, comp=False)
+    part = run_f32(part, p, 13, kernel=2, comp=False, step0=7)
+    assert np.array_equal(whole, part)
+    del torch
+
+
+def test_sliding_rejects_unsupported_shapes():
+    import torch
+    N = native()
+    p = Params(T=0.0, **AMB)
+    a = torch.zeros((32, 100), dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    s = N.amb_stencil(p.dt, p.dx, p.dy)
+    m = N.amb_model(p.a, p.b, p.c, p.kappa, p.lamb, p.zeta, p.T)
+    cfg = N.amb_kernel_config(2, 0, 0, 0)
+    rc = N.lib().amb_step_f32_ex(ctypes.byref(s), ctypes.byref(m), 0, 32, 100, a.data_ptr(), b.data_ptr(), None, 0, 1,
+                                 None, ctypes.byref(cfg), torch.cuda.current_stream().cuda_stream, None)
+    assert rc == N.AMB_ERR_UNSUPPORTED
+    cfg = N.amb_kernel_config(0, 0, 0, 0)  # auto falls back to the tile kernel
+    rc = N.lib().amb_step_f32_ex(ctypes.byref(s), ctypes.byref(m), 0, 32, 100, a.data_ptr(), b.data_ptr(), None, 0, 1,
+                                 None, ctypes.byref(cfg), torch.cuda.current_stream().cuda_stream, None)
+    assert rc == 0
