@@ -120,11 +120,10 @@ namespace amb
         float ua = float(ka + 1u) * (1.0f / 16777216.0f);
         float v = float(16777215u - ka) * (1.0f / 16777216.0f);
         float ub = float(xb >> 8) * (1.0f / 16777216.0f);
-        float t;
-        if (v < 0.03125f)
-            t = 2.0f * v * (1.0f + v * (0.5f + v * (0.333333343f + v * (0.25f + v * 0.2f))));
-        else
-            t = -2.0f * __logf(ua);
+        // both branches evaluated and selected: a divergent branch would make most warps run both anyway
+        float t_series = 2.0f * v * (1.0f + v * (0.5f + v * (0.333333343f + v * (0.25f + v * 0.2f))));
+        float t_log = -2.0f * __logf(ua);
+        float t = v < 0.03125f ? t_series : t_log;
         float r = t * rsqrtf(fmaxf(t, 1e-30f));
         float s, c;
         __sincosf(6.283185307179586f * (ub - 0.5f), &s, &c);

@@ -259,6 +259,8 @@ namespace amb
                 fz[q] = sm.phi[1][own - 1 + q];
             }
             // Rounds are not unrolled (code size): the row rings live in shared memory.
+            float xin[4];    // xi_y of this round's J1_y row, formed one round ahead
+            normals<NOISE>(p, k, injected, wrap_index(t.r0 - 12, ny), gcol, 0, xin);
             int ms = 1;      // mu_p ring slot of row kl  (kl mod 10)
             int js = 6;      // J1_y ring slot of row kl-4 ((kl - 4) mod 9)
 #pragma unroll 1
@@ -325,8 +327,8 @@ namespace amb
                 sts4(&h[1][4 * lane], jcy);
                 sts4(&h[2][4 * lane], jcx);
                 // ---- J1_y at local row kl-4 from mu_p rows kl-8..kl (this lane's own columns).
-                // Outputs start at local row 9; their D8_y reads J1_y rows >= 5, formed from round 9 on.
-                if (kl >= 9)
+                // Outputs start at local row 9 and read J1_y rows >= 5 (rounds >= 9); earlier rounds
+                // compute values nobody reads, which keeps the round one straight-line block.
                 {
                     float m[9][4];
 #pragma unroll
@@ -340,8 +342,9 @@ namespace amb
                     }
 #pragma unroll
                     for (int q = 0; q < 4; ++q) m[8][q] = mup[q];
-                    float xi[4];
-                    normals<NOISE>(p, k, injected, wrap_index(t.r0 - 13 + kl, ny), gcol, 0, xi);
+                    float xi[4] = {xin[0], xin[1], xin[2], xin[3]};
+                    // noise of the next round's J1_y row, formed now so its Philox chain overlaps this round
+                    normals<NOISE>(p, k, injected, wrap_index(t.r0 - 12 + kl, ny), gcol, 0, xin);
                     float j1y[4];
 #pragma unroll
                     for (int q = 0; q < 4; ++q)
@@ -353,8 +356,7 @@ namespace amb
                         j1y[q] = fmaf(k.mag, xi[q], s);
                     }
                     sts4(&sm.j1y[js][4 * lane], j1y);
-                    // ---- DY8 at local row kl-8 from J1_y rows kl-12..kl-4 (outputs from round 17)
-                    if (kl >= 17)
+                    // ---- DY8 at local row kl-8 from J1_y rows kl-12..kl-4 (read by outputs from round 17)
                     {
                         float j[9][4];
 #pragma unroll
@@ -412,6 +414,12 @@ namespace amb
 
             float sxm[3][4], dxm[3][4], sxj[3][4], dxj[3][4];
             float jcy[4], jcx[4];
+            // xi_x and bf16 residual of the output row, fetched one round ahead (round 1 outputs row -7)
+            float xnx[4];
+            normals<NOISE>(p, k, injected, wrap_index(t.r0 - 16, ny), gcol, 1, xnx);
+            uint2 rnext = make_uint2(0u, 0u);
+            if constexpr (COMP == COMP_BF16)
+                rnext = *reinterpret_cast<const uint2*>(residual + (size_t)wrap_index(t.r0 - 16, ny) * nx + gcol);
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -429,9 +437,7 @@ namespace amb
                     if (kl > total) break;
                     pair_sync(bar_id);
                     const float(*h)[kCols] = sm.hand[kl & 1];
-                    // ---- Tjhung chain: J2 at row kl-1, divTj at row kl-2 (first needed: divTj of row 9,
-                    // from mu_a rows >= 7)
-                    if (kl >= 7)
+                    // ---- Tjhung chain: J2 at row kl-1, divTj at row kl-2 (first needed: divTj of row 9)
                     {
                         float4 m4 = lds4(&h[0][4 * lane]);
                         float mL = __shfl_up_sync(0xffffffffu, m4.w, 1);
@@ -475,18 +481,24 @@ namespace amb
                         }
                         sts4(&sm.dtj[(kl - 2) & (kDelay - 1)][4 * lane], dtj);
                     }
-                    // ---- output local row kl-8 (global r0 - 17 + kl)
-                    if (kl >= 17)
+                    // ---- output local row kl-8 (global r0 - 17 + kl); rounds before 17 run the same
+                    // code on rows nobody reads and store nothing
                     {
                         const int lo = kl - 8;
-                        const float* mrow = sm.mup[lo % kMupRing];
+                        const bool store = out_lane && kl >= 17;
+                        const float* mrow = sm.mup[(lo + kMupRing) % kMupRing];
                         float4 ml = lds4(&mrow[(4 * lane - 4) & (kCols - 1)]);
                         float4 mc = lds4(&mrow[4 * lane]);
                         float4 mr = lds4(&mrow[(4 * lane + 4) & (kCols - 1)]);
                         float mu[12] = {ml.x, ml.y, ml.z, ml.w, mc.x, mc.y, mc.z, mc.w, mr.x, mr.y, mr.z, mr.w};
-                        float xi[4];
+                        float xi[4] = {xnx[0], xnx[1], xnx[2], xnx[3]};
                         const int grow = wrap_index(t.r0 - 9 + lo, ny);
-                        normals<NOISE>(p, k, injected, grow, gcol, 1, xi);
+                        // next round's xi_x and residual are fetched now, off this round's critical path
+                        const int grow_next = wrap_index(t.r0 - 8 + lo, ny);
+                        normals<NOISE>(p, k, injected, grow_next, gcol, 1, xnx);
+                        uint2 rv = rnext;
+                        if constexpr (COMP == COMP_BF16)
+                            rnext = *reinterpret_cast<const uint2*>(residual + (size_t)grow_next * nx + gcol);
                         float j1x[4];
 #pragma unroll
                         for (int q = 0; q < 4; ++q)
@@ -512,14 +524,10 @@ namespace amb
                         float rr[4] = {0.f, 0.f, 0.f, 0.f};
                         if constexpr (COMP == COMP_BF16)
                         {
-                            if (out_lane)
-                            {
-                                uint2 rv = *reinterpret_cast<const uint2*>(residual + gi);
-                                rr[0] = __uint_as_float(rv.x << 16);
-                                rr[1] = __uint_as_float(rv.x & 0xffff0000u);
-                                rr[2] = __uint_as_float(rv.y << 16);
-                                rr[3] = __uint_as_float(rv.y & 0xffff0000u);
-                            }
+                            rr[0] = __uint_as_float(rv.x << 16);
+                            rr[1] = __uint_as_float(rv.x & 0xffff0000u);
+                            rr[2] = __uint_as_float(rv.y << 16);
+                            rr[3] = __uint_as_float(rv.y & 0xffff0000u);
                         }
                         float nf[4], nr[4];
 #pragma unroll
@@ -545,7 +553,7 @@ namespace amb
                         }
                         if (*reinterpret_cast<volatile int*>(&sm.abort))
                             nf[0] = nf[1] = nf[2] = nf[3] = __int_as_float(0x7fc00000);
-                        if (out_lane)
+                        if (store)
                         {
                             *reinterpret_cast<float4*>(phi_out + gi) = make_float4(nf[0], nf[1], nf[2], nf[3]);
                             if constexpr (COMP == COMP_BF16)
