@@ -73,6 +73,7 @@ SIGNATURES = {
     "amb_mass_scratch_bytes": (ctypes.c_size_t, [_I64]),
     "amb_mass_f64": (_I, [_VP, _I64, _VP, _VP, ctypes.c_size_t, _VP]),
     "amb_mass_f32": (_I, [_VP, _I64, _VP, _VP, ctypes.c_size_t, _VP]),
+    "amb_mass_f32_noalloc": (_I, [_VP, _I64, _VP, _VP]),
     "amb_check_finite_f64": (_I, [_VP, _I64, _VP, _VP]),
     "amb_check_finite_f32": (_I, [_VP, _I64, _VP, _VP]),
 }

@@ -76,6 +76,8 @@ namespace
     cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 }
 
+void amb::set_last_error(const std::string& msg) { g_last_error = msg; }
+
 extern "C" const char* amb_version(void) { return "amb_gb300 0.1 (sm_103a)"; }
 
 extern "C" const char* amb_last_error(void) { return g_last_error.c_str(); }

@@ -6,6 +6,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <string>
+
 namespace amb
 {
     // Fused single-step tile kernel (amb_step_tile.cuh), one launch = one step.
@@ -31,6 +33,9 @@ namespace amb
 
     template <typename Real>
     cudaError_t launch_nonfinite(const Real* f, size_t n, int* flag, cudaStream_t stream);
+
+    // Sets the message amb_last_error() returns on the calling thread.
+    void set_last_error(const std::string& msg);
 
     cudaError_t launch_convert_f64_to_f32(const double* src, float* dst, size_t n, cudaStream_t stream);
     cudaError_t launch_convert_f32_to_f64(const float* src, double* dst, size_t n, cudaStream_t stream);

@@ -174,6 +174,15 @@ size_t amb_mass_scratch_bytes(int64_t n);
 int amb_mass_f64(const double* field, int64_t n, double* out_sum, void* scratch, size_t scratch_bytes, void* stream);
 int amb_mass_f32(const float* field, int64_t n, double* out_sum, void* scratch, size_t scratch_bytes, void* stream);
 
+/* No counterpart in the reference. amb_mass_f32 without any device allocation, for
+ * callers that cannot allocate (their allocator already holds the device memory, they
+ * only receive device pointers, or they cannot afford cudaMalloc's synchronization).
+ * Scratch is a file-scope device array (256 KiB per GPU, held until process exit);
+ * fields above 2^30 sites are rejected with AMB_ERR_INVALID. The first call on each
+ * device looks up the array's address and should precede any stream capture. All
+ * calls share the array: calls that overlap on the GPU race. */
+int amb_mass_f32_noalloc(const float* field, int64_t n, double* out_sum, void* stream);
+
 /* ORs 1 into *flag (device int) when any element of the field is NaN or Inf
  * (src/integrator.cu:265-272). The caller zeroes the flag. */
 int amb_check_finite_f64(const double* field, int64_t n, int* flag, void* stream);
