@@ -60,6 +60,8 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--temperature", type=float, default=0.05)
+    ap.add_argument("--launches", type=int, default=0,
+                    help="profiling driver: run this many bare step launches through the C ABI and exit")
     return ap.parse_args()
 
 
@@ -194,6 +196,26 @@ def cpu_baseline(w, seconds: float = 10.0, use_reference: bool = True):
     sites = w["ny"] * w["nx"]
     return {"value": nsteps * sites / dt / 1e9, "unit": UNIT, "cores": cores, "kind": kind,
             "sample": f"{nsteps} Euler steps of the {w['ny']}x{w['nx']} workload ({dt:.1f} s); {desc}"}
+
+
+def reference_gpu_baseline(w, nsteps: int = 20):
+    """The reference's own CUDA integrator (FP64, 3 launches per step) on this GPU, timed with
+    CUDA events over nsteps of its run loop on the same workload."""
+    import oracle
+    if not oracle.ReferenceGpuIntegrator.available():
+        return {"unavailable": "reference cubin not built (oracle/build.py needs the reference checkout)"}
+    p = oracle.Params(dt=w["dt"], dx=w["dx"], dy=w["dy"], a=w["a"], b=w["b"], c=w["c"], kappa=w["kappa"],
+                      lamb=w["lamb"], zeta=w["zeta"], T=w["T"])
+    ref = oracle.ReferenceGpuIntegrator(initial_field(w), p, seed=1)
+    try:
+        ref.time_steps(3)
+        ms = ref.time_steps(nsteps)
+    finally:
+        ref.close()
+    sites = w["ny"] * w["nx"]
+    return {"value": nsteps * sites / (ms / 1e3) / 1e9, "unit": UNIT, "dtype": "f64",
+            "sample": f"{nsteps} steps of src/integrator.cu's run loop (step + calculate_forces + "
+                      f"calculate_local_currents) at {w['ny']}x{w['nx']}, CUDA events"}
 
 
 # ------------------------------------------------------------------ arms
@@ -340,7 +362,35 @@ def run_ours(args, w, rank, world, dist):
     }
     if not args.no_cpu and world == 1:
         line["cpu_baseline"] = cpu_baseline(w)
+        line["reference_gpu"] = reference_gpu_baseline(w)
     print(json.dumps(line), flush=True)
+
+
+def run_launches(args, w):
+    """Bare step launches (amb_step_f32_ex / amb_step_f64) on a device field, for profilers."""
+    import torch
+    from activemodelbplus.integrator import _native as N
+    L = N.lib()
+    field = initial_field(w)
+    dtype = torch.float64 if args.precision == "f64" else torch.float32
+    a = torch.from_numpy(field).to(device="cuda", dtype=dtype)
+    b = torch.empty_like(a)
+    s = N.amb_stencil(w["dt"], w["dx"], w["dy"])
+    m = N.amb_model(w["a"], w["b"], w["c"], w["kappa"], w["lamb"], w["zeta"], w["T"])
+    stream = torch.cuda.current_stream().cuda_stream
+    if args.precision == "f64":
+        rc = L.amb_step_f64(ctypes.byref(s), ctypes.byref(m), 1, w["ny"], w["nx"], a.data_ptr(), b.data_ptr(), 0,
+                            args.launches, None, stream, None)
+    else:
+        res = torch.zeros(a.shape, dtype=torch.int16, device="cuda") if args.precision == "f32c" else None
+        cfg = N.amb_kernel_config({"auto": 0, "tile": 1, "sliding": 2}[args.kernel], 0, 0, 0)
+        rc = L.amb_step_f32_ex(ctypes.byref(s), ctypes.byref(m), 1, w["ny"], w["nx"], a.data_ptr(), b.data_ptr(),
+                               res.data_ptr() if res is not None else None, 0, args.launches, None, ctypes.byref(cfg),
+                               stream, None)
+    torch.cuda.synchronize()
+    if rc:
+        raise RuntimeError(N.last_error())
+    print(json.dumps({"launches": args.launches, "size": w["ny"], "precision": args.precision}))
 
 
 def main():
@@ -350,6 +400,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     w = workload(args)
+    if args.launches > 0:
+        return run_launches(args, w)
     if args.impl == "reference":
         return run_reference_arm(args, w, rank, world)
     import torch

@@ -200,3 +200,71 @@ def tjhung_run(phi, nsteps: int, dt: float, h: float, A: float, K: float, lamb: 
     if rc:
         raise ValueError("tjhung_ref_run rejected the arguments")
     return phi
+
+
+# ------------------------------------------------- the reference's own CUDA integrator
+
+class ReferenceGpuIntegrator:
+    """The reference's CUDA Integrator (src/integrator.cu) run from its compiled cubin
+    (oracle/_ref/ref_integrator.cubin) by oracle/ref_gpu_driver.cc: FP64, three launches per
+    step, curand XORWOW noise seeded with ``seed``. Baseline and parity infrastructure."""
+
+    _lib = None
+
+    @classmethod
+    def available(cls) -> bool:
+        return os.path.exists(_build.REF_GPU_CUBIN)
+
+    @classmethod
+    def _load(cls):
+        if cls._lib is None:
+            path = _build.build_ref_gpu_driver()
+            L = ctypes.CDLL(path)
+            L.refgpu_last_error.restype = ctypes.c_char_p
+            L.refgpu_load.argtypes = [ctypes.c_char_p]
+            L.refgpu_create.argtypes = [_DP, ctypes.c_int, ctypes.c_int, _DP, _DP, ctypes.c_ulonglong,
+                                        ctypes.POINTER(ctypes.c_void_p)]
+            L.refgpu_run.argtypes = [ctypes.c_void_p, ctypes.c_int]
+            L.refgpu_get_field.argtypes = [ctypes.c_void_p, _DP]
+            L.refgpu_time_steps.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+            L.refgpu_destroy.argtypes = [ctypes.c_void_p]
+            if L.refgpu_load(_build.REF_GPU_CUBIN.encode()):
+                raise RuntimeError(L.refgpu_last_error().decode())
+            cls._lib = L
+        return cls._lib
+
+    def __init__(self, field, p: Params, seed: int = 0):
+        L = self._load()
+        f = _f64(field)
+        self.shape = f.shape
+        st = np.array([p.dt, p.dx, p.dy])
+        md = np.array([p.a, p.b, p.c, p.kappa, p.lamb, p.zeta, p.T])
+        self._h = ctypes.c_void_p()
+        if L.refgpu_create(_ptr(f), f.shape[0], f.shape[1], _ptr(st), _ptr(md), seed, ctypes.byref(self._h)):
+            raise RuntimeError(L.refgpu_last_error().decode())
+
+    def run(self, nsteps: int) -> None:
+        rc = self._lib.refgpu_run(self._h, nsteps)
+        if rc:
+            raise RuntimeError(self._lib.refgpu_last_error().decode())
+
+    def time_steps(self, nsteps: int) -> float:
+        """Milliseconds (CUDA events) for nsteps of the run loop."""
+        ms = ctypes.c_float()
+        if self._lib.refgpu_time_steps(self._h, nsteps, ctypes.byref(ms)):
+            raise RuntimeError(self._lib.refgpu_last_error().decode())
+        return ms.value
+
+    @property
+    def field(self) -> np.ndarray:
+        out = np.empty(self.shape)
+        if self._lib.refgpu_get_field(self._h, _ptr(out)):
+            raise RuntimeError(self._lib.refgpu_last_error().decode())
+        return out
+
+    def close(self):
+        if self._h:
+            self._lib.refgpu_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    __del__ = close

@@ -22,6 +22,9 @@ REF_DIR = os.path.join(HERE, "_ref")
 REFERENCE_ROOT = os.environ.get("AMB_REFERENCE_ROOT", "/root/reference")
 
 ORACLE_LIB = os.path.join(BUILD_DIR, "libamb_oracle.so")
+REF_GPU_DRIVER = os.path.join(BUILD_DIR, "libref_gpu_driver.so")
+REF_GPU_CUBIN = os.path.join(REF_DIR, "ref_integrator.cubin")
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 TJHUNG_LIB = os.path.join(REF_DIR, "libtjhung_ref.so")
 TJHUNG_FAST_LIB = os.path.join(REF_DIR, "libtjhung_ref_fast.so")
 
@@ -74,9 +77,50 @@ def build_reference(force: bool = False) -> list[str]:
     return built
 
 
+def build_reference_gpu_cubin(force: bool = False) -> str | None:
+    """The reference's own device code (src/integrator.cu + src/parameters.cu), compiled with its
+    CMake flags (CMakeLists.txt:15-22) for sm_103a and device-linked into one cubin. Only where
+    the reference checkout exists; the cubin then travels with the repository copy."""
+    if not reference_available():
+        return REF_GPU_CUBIN if os.path.exists(REF_GPU_CUBIN) else None
+    srcs = [os.path.join(REFERENCE_ROOT, "src", f) for f in ("integrator.cu", "parameters.cu")]
+    if not force and not _stale(REF_GPU_CUBIN, srcs + [__file__]):
+        return REF_GPU_CUBIN
+    os.makedirs(REF_DIR, exist_ok=True)
+    nvcc = os.path.join(CUDA_HOME, "bin", "nvcc")
+    objs = []
+    for src in srcs:
+        obj = os.path.join(REF_DIR, os.path.basename(src) + ".rdc.cubin")
+        _run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++20", "-O3", "--expt-relaxed-constexpr",
+              "-diag-suppress", "20012", "--use_fast_math", "-ftz=true", "-prec-div=false", "-prec-sqrt=false",
+              "-rdc=true", "-cubin", "-I", os.path.join(REFERENCE_ROOT, "src"), "-I", os.path.join(HERE, "eigen_standin"),
+              src, "-o", obj])
+        objs.append(obj)
+    tmp = REF_GPU_CUBIN + f".tmp{os.getpid()}"
+    _run([os.path.join(CUDA_HOME, "bin", "nvlink"), "--arch=sm_103a", *objs, "-o", tmp])
+    os.replace(tmp, REF_GPU_CUBIN)
+    for o in objs:
+        os.remove(o)
+    return REF_GPU_CUBIN
+
+
+def build_ref_gpu_driver(force: bool = False) -> str:
+    """Host driver (our own code, CUDA driver API) that runs the reference's cubin."""
+    src = os.path.join(HERE, "ref_gpu_driver.cc")
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if force or _stale(REF_GPU_DRIVER, [src, __file__]):
+        tmp = REF_GPU_DRIVER + f".tmp{os.getpid()}"
+        _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-I", os.path.join(CUDA_HOME, "include"), src,
+              "-o", tmp, "-L", os.path.join(CUDA_HOME, "lib64", "stubs"), "-lcuda"])
+        os.replace(tmp, REF_GPU_DRIVER)
+    return REF_GPU_DRIVER
+
+
 def build_all(force: bool = False) -> None:
     build_oracle(force)
     build_reference(force)
+    build_reference_gpu_cubin(force)
+    build_ref_gpu_driver(force)
 
 
 if __name__ == "__main__":
