@@ -74,6 +74,9 @@ SIGNATURES = {
     "amb_mass_f64": (_I, [_VP, _I64, _VP, _VP, ctypes.c_size_t, _VP]),
     "amb_mass_f32": (_I, [_VP, _I64, _VP, _VP, ctypes.c_size_t, _VP]),
     "amb_mass_f32_noalloc": (_I, [_VP, _I64, _VP, _VP]),
+    "amb_radial_spectrum": (_I, [_VP, _I, _I, ctypes.c_double, ctypes.c_double, _VP, _I, _VP, _VP, _VP]),
+    "amb_label_components_f64": (_I, [_VP, _I, _I, ctypes.c_double, _VP, _VP, _VP]),
+    "amb_label_components_f32": (_I, [_VP, _I, _I, ctypes.c_double, _VP, _VP, _VP]),
     "amb_check_finite_f64": (_I, [_VP, _I64, _VP, _VP]),
     "amb_check_finite_f32": (_I, [_VP, _I64, _VP, _VP]),
 }

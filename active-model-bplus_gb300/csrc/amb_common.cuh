@@ -95,20 +95,10 @@ namespace amb
         return philox4x32_10(ctr, uint32_t(seed), uint32_t(seed >> 32));
     }
 
-    // Box-Muller on one pair of 32-bit words, 24-bit uniforms:
+    // Box-Muller on one pair of 32-bit words with 24-bit uniforms:
     // ua = ((xa >> 8) + 1) 2^-24 in (0,1], ub = (xb >> 8) 2^-24 in [0,1);
     // r = sqrt(-2 ln ua), theta = 2 pi (ub - 1/2); returns (r cos theta, r sin theta).
-    __device__ __forceinline__ double2 box_muller_f64(uint32_t xa, uint32_t xb)
-    {
-        double ua = (double((xa >> 8) + 1u)) * (1.0 / 16777216.0);
-        double ub = double(xb >> 8) * (1.0 / 16777216.0);
-        double r = sqrt(-2.0 * log(ua));
-        double s, c;
-        sincospi(2.0 * (ub - 0.5), &s, &c);
-        return make_double2(r * c, r * s);
-    }
-
-    // Single-precision counterpart of the same definition. -ln(ua) uses the fast
+    // Evaluated in single precision. -ln(ua) uses the fast
     // hardware logarithm (__logf) where ua <= 31/32; closer to 1 its absolute
     // error would rival ln(ua) itself, so there -ln(1 - v), v = 1 - ua (exact),
     // is summed from the Mercator series v + v^2/2 + ... + v^5/5 (truncation
@@ -130,40 +120,25 @@ namespace amb
         return make_float2(r * c, r * s);
     }
 
-    // One standard normal of the (seed, step) noise field at (row, col, comp).
-    template <typename Real>
-    __device__ __forceinline__ Real noise_normal(uint64_t seed, int64_t step, int row, int col, int comp)
+    // One standard normal of the (seed, step) noise field at (row, col, comp). Both field
+    // precisions draw the same single-precision Box-Muller normals: the noise only needs
+    // statistical accuracy, and GB300's FP64 rate would make a double-precision transform
+    // cost more than the stencil itself.
+    __device__ __forceinline__ float noise_normal(uint64_t seed, int64_t step, int row, int col, int comp)
     {
         U4 q = noise_bits(seed, step, row, col, comp);
         int lane = col & 3;
         uint32_t xa = (lane < 2) ? q.x : q.z;
         uint32_t xb = (lane < 2) ? q.y : q.w;
-        if constexpr (sizeof(Real) == 8)
-        {
-            double2 z = box_muller_f64(xa, xb);
-            return (lane & 1) ? z.y : z.x;
-        }
-        else
-        {
-            float2 z = box_muller_f32(xa, xb);
-            return (lane & 1) ? z.y : z.x;
-        }
+        float2 z = box_muller_f32(xa, xb);
+        return (lane & 1) ? z.y : z.x;
     }
 
-    // All four normals of a quad (columns 4q..4q+3).
-    template <typename Real>
-    __device__ __forceinline__ void noise_quad(uint64_t seed, int64_t step, int row, int col4, int comp, Real z[4])
+    // All four normals of a quad (columns 4q..4q+3; col4 is any column of the quad).
+    __device__ __forceinline__ void noise_quad(uint64_t seed, int64_t step, int row, int col4, int comp, float z[4])
     {
         U4 q = noise_bits(seed, step, row, col4, comp);
-        if constexpr (sizeof(Real) == 8)
-        {
-            double2 p0 = box_muller_f64(q.x, q.y), p1 = box_muller_f64(q.z, q.w);
-            z[0] = p0.x; z[1] = p0.y; z[2] = p1.x; z[3] = p1.y;
-        }
-        else
-        {
-            float2 p0 = box_muller_f32(q.x, q.y), p1 = box_muller_f32(q.z, q.w);
-            z[0] = p0.x; z[1] = p0.y; z[2] = p1.x; z[3] = p1.y;
-        }
+        float2 p0 = box_muller_f32(q.x, q.y), p1 = box_muller_f32(q.z, q.w);
+        z[0] = p0.x; z[1] = p0.y; z[2] = p1.x; z[3] = p1.y;
     }
 }

@@ -177,31 +177,58 @@ namespace amb
         }
         __syncthreads();
 
-        // Stage 2: J1 = J_p + J_r on the two arms, J2 = J_l + J_c on the box.
+        // Stage 2: J1 = J_p + J_r on the two arms, J2 = J_l + J_c on the box. With Philox
+        // noise and ncols % 4 == 0 the arms are walked by column quads, one Philox call per
+        // quad (the tile origin is a multiple of 4, so quads align with the noise's quads).
         const size_t plane = (size_t)ny * nx;
-        for (int e = tid; e < G::PY * TX; e += nthr)
+        if (noise_mode == NOISE_PHILOX && nx % 4 == 0)
         {
-            int i = e / TX - 4, j = e % TX;
-            Real xi = 0;
-            if (noise_mode != NOISE_OFF)
+            constexpr int QY = TX / 4, QQ = G::QX / 4;
+            for (int e = tid; e < G::PY * QY; e += nthr)
             {
-                int gr = wrap_index(r0 + i, ny), gc = wrap_index(c0 + j, nx);
-                xi = noise_mode == NOISE_PHILOX ? noise_normal<Real>(p.seed, p.step, gr, gc, 0)
-                                                : injected[(size_t)gr * nx + gc];
+                int i = e / QY - 4, j = (e % QY) * 4;
+                float z[4];
+                noise_quad(p.seed, p.step, wrap_index(r0 + i, ny), wrap_index(c0 + j, nx), 0, z);
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    J1Y[(i + 4) * TX + j + q] = -(k.dyInv * d8_y(MUP, G::MX, i + 8, j + q + 8)) + k.mag * Real(z[q]);
             }
-            J1Y[e] = -(k.dyInv * d8_y(MUP, G::MX, i + 8, j + 8)) + k.mag * xi;
+            for (int e = tid; e < TY * QQ; e += nthr)
+            {
+                int i = e / QQ, j = (e % QQ) * 4 - 4;
+                float z[4];
+                noise_quad(p.seed, p.step, wrap_index(r0 + i, ny), wrap_index(c0 + j, nx), 1, z);
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    J1X[i * G::QX + j + q + 4] = -(k.dxInv * d8_x(MUP, G::MX, i + 8, j + q + 8)) + k.mag * Real(z[q]);
+            }
         }
-        for (int e = tid; e < TY * G::QX; e += nthr)
+        else
         {
-            int i = e / G::QX, j = e % G::QX - 4;
-            Real xi = 0;
-            if (noise_mode != NOISE_OFF)
+            for (int e = tid; e < G::PY * TX; e += nthr)
             {
-                int gr = wrap_index(r0 + i, ny), gc = wrap_index(c0 + j, nx);
-                xi = noise_mode == NOISE_PHILOX ? noise_normal<Real>(p.seed, p.step, gr, gc, 1)
-                                                : injected[plane + (size_t)gr * nx + gc];
+                int i = e / TX - 4, j = e % TX;
+                Real xi = 0;
+                if (noise_mode != NOISE_OFF)
+                {
+                    int gr = wrap_index(r0 + i, ny), gc = wrap_index(c0 + j, nx);
+                    xi = noise_mode == NOISE_PHILOX ? Real(noise_normal(p.seed, p.step, gr, gc, 0))
+                                                    : injected[(size_t)gr * nx + gc];
+                }
+                J1Y[e] = -(k.dyInv * d8_y(MUP, G::MX, i + 8, j + 8)) + k.mag * xi;
             }
-            J1X[e] = -(k.dxInv * d8_x(MUP, G::MX, i + 8, j + 8)) + k.mag * xi;
+            for (int e = tid; e < TY * G::QX; e += nthr)
+            {
+                int i = e / G::QX, j = e % G::QX - 4;
+                Real xi = 0;
+                if (noise_mode != NOISE_OFF)
+                {
+                    int gr = wrap_index(r0 + i, ny), gc = wrap_index(c0 + j, nx);
+                    xi = noise_mode == NOISE_PHILOX ? Real(noise_normal(p.seed, p.step, gr, gc, 1))
+                                                    : injected[plane + (size_t)gr * nx + gc];
+                }
+                J1X[e] = -(k.dxInv * d8_x(MUP, G::MX, i + 8, j + 8)) + k.mag * xi;
+            }
         }
         for (int e = tid; e < G::CY * G::CX; e += nthr)
         {

@@ -51,8 +51,8 @@ namespace amb
             double xy = 0, xx = 0;
             if (noise_mode == 1)
             {
-                xy = double(noise_normal<Real>(p.seed, p.step, r, c, 0));
-                xx = double(noise_normal<Real>(p.seed, p.step, r, c, 1));
+                xy = double(noise_normal(p.seed, p.step, r, c, 0));
+                xx = double(noise_normal(p.seed, p.step, r, c, 1));
             }
             else if (noise_mode == 2)
             {

@@ -188,6 +188,25 @@ int amb_mass_f32_noalloc(const float* field, int64_t n, double* out_sum, void* s
 int amb_check_finite_f64(const double* field, int64_t n, int* flag, void* stream);
 int amb_check_finite_f32(const float* field, int64_t n, int* flag, void* stream);
 
+/* ================================================================ analysis */
+
+/* Radial binning of a power spectrum (device arrays). power: nrows*ncols values |phi_q|^2 in
+ * FFT order; mode (r, c) has |k| from numpy's fftfreq convention with spacings dx, dy. Adds
+ * each mode to bin l with edges[l-1] < |k| <= edges[l] (np.digitize right=True, the binning of
+ * the reference's analysis notebook examples/structureFactor.ipynb); sum[l] and count[l]
+ * (nedges each) are zeroed first. */
+int amb_radial_spectrum(const double* power, int nrows, int ncols, double dx, double dy, const double* edges,
+                        int nedges, double* sum, unsigned long long* count, void* stream);
+
+/* 4-connected components of {field > threshold} on the periodic grid (no reference
+ * counterpart; the droplet count of the analysis). labels: nrows*ncols ints, set to the
+ * smallest linear index of each site's component, -1 for background. *ncomp (device int)
+ * receives the number of components. Grids below 2^31 sites. */
+int amb_label_components_f64(const double* field, int nrows, int ncols, double threshold, int* labels, int* ncomp,
+                             void* stream);
+int amb_label_components_f32(const float* field, int nrows, int ncols, double threshold, int* labels, int* ncomp,
+                             void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -35,8 +35,9 @@
  * non-deterministically, src/integrator.cu:275-282,320-323): standard normals
  * xi keyed on (seed, step, site, component) by Philox4x32-10 (Salmon, Moraes,
  * Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC'11) and
- * Box-Muller. The definition is restated in orc_noise_normal() below and is
- * the one the CUDA kernels implement.
+ * Box-Muller. The definition is restated in orc_noise_normal() below (in
+ * double precision); the CUDA kernels evaluate the same definition in single
+ * precision, within 5e-5 of it.
  */
 #include <math.h>
 #include <stdint.h>
