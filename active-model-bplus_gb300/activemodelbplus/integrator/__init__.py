@@ -27,7 +27,8 @@ import numpy as np
 
 from . import _native as N
 
-__all__ = ["Model", "Stencil", "Integrator", "CudaException", "steps_from_time", "step_iterator", "plot_field"]
+__all__ = ["Model", "Stencil", "Integrator", "Ensemble", "CudaException", "steps_from_time", "step_iterator",
+           "plot_field"]
 
 
 class CudaException(RuntimeError):
@@ -487,6 +488,89 @@ class Integrator:
         assert (self.timestep - initial_timestep) == nsteps
         if t_interrupt is not None and np.any(np.isclose(self.time - initial_time, t_interrupt)):
             f_interrupt(self)
+
+
+# ------------------------------------------------------------------ ensemble
+
+class Ensemble:
+    """Many independent replicas advanced together on one GPU (no reference counterpart).
+
+    Each replica has its own field (any size with ncols >= 112 and ncols % 4 == 0), stencil,
+    model and Philox seed; storage is FP32 ("f32") or compensated FP32 ("f32c"). One kernel
+    launch per step covers every replica, and ``graph_steps`` steps are captured once into a
+    CUDA graph and replayed (C ABI ``amb_ensemble_*``).
+    """
+
+    def __init__(self, fields, stencils, models, *, precision: str = "f32c", seeds=None, graph_steps: int = 64):
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise CudaException("no CUDA device is available")
+        L = N.lib()
+        fields = [np.ascontiguousarray(np.asarray(f, dtype=np.float64)) for f in fields]
+        n = len(fields)
+        if n == 0:
+            raise ValueError("an ensemble needs at least one replica")
+        stencils = [Stencil(stencils)] * n if isinstance(stencils, Stencil) else [Stencil(s) for s in stencils]
+        models = [Model(models)] * n if isinstance(models, Model) else [Model(m) for m in models]
+        if len(stencils) != n or len(models) != n:
+            raise ValueError("one stencil and one model per replica (or a single shared one)")
+        if precision not in ("f32", "f32c"):
+            raise ValueError("ensemble precision must be 'f32' or 'f32c'")
+        seeds = [_random_seed() for _ in range(n)] if seeds is None else [int(x) & 0xFFFFFFFFFFFFFFFF for x in seeds]
+        self._shapes = [f.shape for f in fields]
+        self._seeds = seeds
+        nrows = (ctypes.c_int * n)(*[f.shape[0] for f in fields])
+        ncols = (ctypes.c_int * n)(*[f.shape[1] for f in fields])
+        ptrs = (ctypes.POINTER(ctypes.c_double) * n)(*[f.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for f in fields])
+        st = (N.amb_stencil * n)(*[N.stencil_struct(s) for s in stencils])
+        md = (N.amb_model * n)(*[N.model_struct(m) for m in models])
+        sd = (ctypes.c_uint64 * n)(*seeds)
+        self._h = ctypes.c_void_p()
+        _check(L.amb_ensemble_create(n, nrows, ncols, ptrs, st, md, sd, _PRECISIONS[precision], int(graph_steps),
+                                     ctypes.byref(self._h)))
+
+    def run(self, nsteps: int) -> None:
+        _check(N.lib().amb_ensemble_run(self._h, int(nsteps)))
+
+    def field(self, replica: int) -> np.ndarray:
+        out = np.empty(self._shapes[replica])
+        _check(N.lib().amb_ensemble_get_field(self._h, int(replica), out.ctypes.data))
+        return out
+
+    @property
+    def fields(self):
+        return [self.field(r) for r in range(len(self._shapes))]
+
+    def _info(self):
+        ts, nt, sr = ctypes.c_int64(), ctypes.c_int(), ctypes.c_int()
+        _check(N.lib().amb_ensemble_info(self._h, ctypes.byref(ts), ctypes.byref(nt), ctypes.byref(sr)))
+        return ts.value, nt.value, sr.value
+
+    @property
+    def timestep(self) -> int:
+        return self._info()[0]
+
+    @property
+    def ntasks(self) -> int:
+        return self._info()[1]
+
+    @property
+    def seeds(self):
+        return list(self._seeds)
+
+    def __len__(self):
+        return len(self._shapes)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().amb_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ------------------------------------------------------------------ helpers

@@ -74,6 +74,12 @@ SIGNATURES = {
     "amb_mass_f64": (_I, [_VP, _I64, _VP, _VP, ctypes.c_size_t, _VP]),
     "amb_mass_f32": (_I, [_VP, _I64, _VP, _VP, ctypes.c_size_t, _VP]),
     "amb_mass_f32_noalloc": (_I, [_VP, _I64, _VP, _VP]),
+    "amb_ensemble_create": (_I, [_I, _IP, _IP, ctypes.POINTER(ctypes.POINTER(ctypes.c_double)), _SP, _MP,
+                                 ctypes.POINTER(ctypes.c_uint64), _I, _I, ctypes.POINTER(_VP)]),
+    "amb_ensemble_destroy": (None, [_VP]),
+    "amb_ensemble_run": (_I, [_VP, _I]),
+    "amb_ensemble_get_field": (_I, [_VP, _I, _VP]),
+    "amb_ensemble_info": (_I, [_VP, ctypes.POINTER(_I64), _IP, _IP]),
     "amb_radial_spectrum": (_I, [_VP, _I, _I, ctypes.c_double, ctypes.c_double, _VP, _I, _VP, _VP, _VP]),
     "amb_label_components_f64": (_I, [_VP, _I, _I, ctypes.c_double, _VP, _VP, _VP]),
     "amb_label_components_f32": (_I, [_VP, _I, _I, ctypes.c_double, _VP, _VP, _VP]),

@@ -137,7 +137,7 @@ extern "C" int amb_step_f32_ex(const amb_stencil* stencil, const amb_model* mode
     if (cfg.kernel == AMB_KERNEL_SLIDING)
     {
         if (!fits)
-            return fail(AMB_ERR_UNSUPPORTED, "sliding kernel needs ncols % 4 == 0, ncols >= 136 and 16-byte aligned "
+            return fail(AMB_ERR_UNSUPPORTED, "sliding kernel needs ncols % 4 == 0, ncols >= 112 and 16-byte aligned "
                                              "field buffers (8-byte residual)");
         sliding = true;
     }

@@ -1,0 +1,285 @@
+// Batched ensemble: many independent replicas (any mix of grid sizes and model
+// parameters, FP32 storage) advanced together. Every step is ONE launch of the
+// warp-pair sliding kernel over a task table that spans all replicas; K steps
+// are captured once into a CUDA graph and replayed, and the step index lives in
+// device memory so the same graph serves every chunk.
+//
+// Task table: each replica is cut into 112-column strips and row segments; the
+// segment height is chosen for the whole ensemble from the device's resident
+// warp-pair count (waves x (rows + pipeline fill) minimised), larger tasks first.
+// The reference has no counterpart: it runs one integrator per process.
+#include "amb_gb300.h"
+#include "amb_kernels.h"
+#include "amb_step_tile.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+struct amb_ensemble
+{
+    int nrep = 0, precision = AMB_F32C, graph_steps = 0, parity = 0;
+    bool noise = false;
+    std::vector<int> ny, nx;
+    std::vector<amb::EnsembleReplica> host_reps;
+    std::vector<void*> allocations;
+    amb::EnsembleReplica* d_reps = nullptr;
+    void* d_coefs = nullptr;
+    amb::EnsembleTask* d_tasks = nullptr;
+    int ntasks = 0, seg_h = 0;
+    int64_t* d_step = nullptr;
+    int64_t step = 0;
+    int* d_flag = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one per starting parity
+};
+
+namespace
+{
+    int efail(int code, const std::string& msg)
+    {
+        amb::set_last_error(msg);
+        return code;
+    }
+
+    int ecuda(cudaError_t e, const char* where)
+    {
+        return efail(AMB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+    }
+
+    __global__ void advance_step_kernel(int64_t* counter, int n) { *counter += n; }
+
+    void release(amb_ensemble* h)
+    {
+        if (!h) return;
+        if (h->stream) cudaStreamSynchronize(h->stream);
+        for (auto g : h->graph)
+            if (g) cudaGraphExecDestroy(g);
+        for (void* p : h->allocations) cudaFree(p);
+        if (h->stream) cudaStreamDestroy(h->stream);
+        delete h;
+    }
+
+    template <typename T>
+    cudaError_t dalloc(amb_ensemble* h, T** p, size_t bytes)
+    {
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, bytes);
+        if (e == cudaSuccess)
+        {
+            h->allocations.push_back(q);
+            *p = static_cast<T*>(q);
+        }
+        return e;
+    }
+
+    // One step for all replicas: launch with the current parity and step offset.
+    cudaError_t launch_step(amb_ensemble* h, int parity, int offset)
+    {
+        return amb::launch_sliding_ensemble(h->d_reps, h->d_coefs, h->d_tasks, h->ntasks, parity, h->d_step, offset,
+                                            h->precision == AMB_F32C ? amb::COMP_BF16 : amb::COMP_NONE,
+                                            h->noise ? amb::NOISE_PHILOX : amb::NOISE_OFF, h->stream);
+    }
+
+    // Capture graph_steps (even) steps from the current parity, and the counter advance,
+    // into one executable graph.
+    int build_graph(amb_ensemble* h)
+    {
+        cudaGraphExec_t* slot = &h->graph[h->parity];
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return ecuda(e, "amb_ensemble graph capture");
+        for (int s = 0; s < h->graph_steps && e == cudaSuccess; ++s) e = launch_step(h, (h->parity + s) & 1, s);
+        if (e == cudaSuccess)
+        {
+            advance_step_kernel<<<1, 1, 0, h->stream>>>(h->d_step, h->graph_steps);
+            e = cudaGetLastError();
+        }
+        cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(slot, g, 0);
+        if (g) cudaGraphDestroy(g);
+        return e == cudaSuccess ? AMB_OK : ecuda(e, "amb_ensemble graph");
+    }
+}
+
+extern "C" int amb_ensemble_create(int nreplicas, const int* nrows, const int* ncols, const double* const* host_fields,
+                                   const amb_stencil* stencils, const amb_model* models, const uint64_t* seeds,
+                                   int precision, int graph_steps, amb_ensemble** out)
+{
+    if (!out) return efail(AMB_ERR_INVALID, "out must not be NULL");
+    *out = nullptr;
+    if (nreplicas < 1 || !nrows || !ncols || !host_fields || !stencils || !models || !seeds)
+        return efail(AMB_ERR_INVALID, "amb_ensemble_create: bad arguments");
+    if (precision != AMB_F32 && precision != AMB_F32C)
+        return efail(AMB_ERR_INVALID, "amb_ensemble_create: precision must be AMB_F32 or AMB_F32C");
+    if (graph_steps < 0 || graph_steps % 2)
+        return efail(AMB_ERR_INVALID, "amb_ensemble_create: graph_steps must be even and >= 0");
+    for (int r = 0; r < nreplicas; ++r)
+        if (nrows[r] < 1 || ncols[r] < 112 || ncols[r] % 4 || !host_fields[r])
+            return efail(AMB_ERR_INVALID, "amb_ensemble_create: replica " + std::to_string(r)
+                                              + " needs nrows >= 1, ncols >= 112 and ncols % 4 == 0");
+
+    auto* h = new (std::nothrow) amb_ensemble;
+    if (!h) return efail(AMB_ERR_NOMEM, "host allocation failed");
+    h->nrep = nreplicas;
+    h->precision = precision;
+    h->graph_steps = graph_steps;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    std::vector<unsigned char> coefs(amb::sliding_coef_bytes() * size_t(nreplicas));
+    for (int r = 0; r < nreplicas && e == cudaSuccess; ++r)
+    {
+        const size_t n = size_t(nrows[r]) * ncols[r];
+        h->ny.push_back(nrows[r]);
+        h->nx.push_back(ncols[r]);
+        amb::EnsembleReplica rep{};
+        for (int b = 0; b < 2 && e == cudaSuccess; ++b) e = dalloc(h, &rep.phi[b], n * sizeof(float));
+        if (e == cudaSuccess && precision == AMB_F32C)
+        {
+            e = dalloc(h, &rep.residual, n * sizeof(uint16_t));
+            if (e == cudaSuccess) e = cudaMemsetAsync(rep.residual, 0, n * sizeof(uint16_t), h->stream);
+        }
+        if (e == cudaSuccess)
+        {
+            std::vector<float> tmp(n);
+            for (size_t i = 0; i < n; ++i) tmp[i] = float(host_fields[r][i]);
+            e = cudaMemcpy(rep.phi[0], tmp.data(), n * sizeof(float), cudaMemcpyHostToDevice);
+        }
+        const amb_stencil& st = stencils[r];
+        const amb_model& md = models[r];
+        amb::StepParams p{};
+        p.ny = nrows[r];
+        p.nx = ncols[r];
+        p.dt = st.dt;
+        p.dxInv = 1 / st.dx;
+        p.dyInv = 1 / st.dy;
+        p.a = md.a; p.b = md.b; p.c = md.c; p.kappa = md.kappa; p.lambda = md.lambda; p.zeta = md.zeta;
+        p.noise_mag = std::sqrt(2 * md.temperature) * std::sqrt(1. / (st.dt * st.dx * st.dy));
+        p.seed = seeds[r];
+        if (md.temperature != 0) h->noise = true;
+        rep.p = p;
+        amb::sliding_make_coef(p, coefs.data() + amb::sliding_coef_bytes() * r);
+        h->host_reps.push_back(rep);
+    }
+
+    // task table
+    int resident = 0;
+    if (e == cudaSuccess) e = amb::ensemble_resident_pairs(&resident);
+    std::vector<amb::EnsembleTask> tasks;
+    if (e == cudaSuccess)
+    {
+        double best = 1e300;
+        for (int H = 16; H <= 1024; H += 8)
+        {
+            long long ntask = 0, rows_max = 0;
+            for (int r = 0; r < nreplicas; ++r)
+            {
+                int h_r = std::min(H, h->ny[r]);
+                ntask += (long long)((h->nx[r] + 111) / 112) * ((h->ny[r] + h_r - 1) / h_r);
+                rows_max = std::max<long long>(rows_max, h_r);
+            }
+            long long waves = (ntask + resident - 1) / resident;
+            double cost = double(waves) * double(H + 10);
+            if (cost < best - 1e-9)
+            {
+                best = cost;
+                h->seg_h = H;
+            }
+        }
+        for (int r = 0; r < nreplicas; ++r)
+        {
+            int h_r = std::min(h->seg_h, h->ny[r]);
+            int strips = (h->nx[r] + 111) / 112;
+            for (int r0 = 0; r0 < h->ny[r]; r0 += h_r)
+                for (int sidx = 0; sidx < strips; ++sidx)
+                    tasks.push_back({r, sidx, r0, std::min(r0 + h_r, h->ny[r])});
+        }
+        std::stable_sort(tasks.begin(), tasks.end(),
+                         [](const amb::EnsembleTask& a, const amb::EnsembleTask& b) { return a.r1 - a.r0 > b.r1 - b.r0; });
+        h->ntasks = int(tasks.size());
+    }
+    if (e == cudaSuccess) e = dalloc(h, &h->d_reps, sizeof(amb::EnsembleReplica) * nreplicas);
+    if (e == cudaSuccess) e = dalloc(h, &h->d_coefs, coefs.size());
+    if (e == cudaSuccess) e = dalloc(h, &h->d_tasks, sizeof(amb::EnsembleTask) * tasks.size());
+    if (e == cudaSuccess) e = dalloc(h, &h->d_step, sizeof(int64_t));
+    if (e == cudaSuccess) e = dalloc(h, &h->d_flag, sizeof(int));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(h->d_reps, h->host_reps.data(), sizeof(amb::EnsembleReplica) * nreplicas, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_coefs, coefs.data(), coefs.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(h->d_tasks, tasks.data(), sizeof(amb::EnsembleTask) * tasks.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(h->d_step, 0, sizeof(int64_t));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess)
+    {
+        int code = e == cudaErrorMemoryAllocation ? AMB_ERR_NOMEM : AMB_ERR_CUDA;
+        release(h);
+        return efail(code, std::string("amb_ensemble_create: ") + cudaGetErrorString(e));
+    }
+    *out = h;
+    return AMB_OK;
+}
+
+extern "C" void amb_ensemble_destroy(amb_ensemble* h) { release(h); }
+
+extern "C" int amb_ensemble_run(amb_ensemble* h, int nsteps)
+{
+    if (!h || nsteps < 0) return efail(AMB_ERR_INVALID, "amb_ensemble_run: bad arguments");
+    cudaError_t e = cudaSuccess;
+    int done = 0;
+    if (h->graph_steps > 0 && nsteps >= h->graph_steps)
+    {
+        if (!h->graph[h->parity])
+            if (int rc = build_graph(h)) return rc;
+        for (; done + h->graph_steps <= nsteps && e == cudaSuccess; done += h->graph_steps)
+            e = cudaGraphLaunch(h->graph[h->parity], h->stream);  // parity unchanged: graph_steps is even
+    }
+    for (int s = 0; done < nsteps && e == cudaSuccess; ++done, ++s)
+    {
+        e = launch_step(h, h->parity, s);
+        h->parity ^= 1;
+        if (e == cudaSuccess && done + 1 == nsteps)
+        {
+            advance_step_kernel<<<1, 1, 0, h->stream>>>(h->d_step, s + 1);
+            e = cudaGetLastError();
+        }
+    }
+    if (e != cudaSuccess) return ecuda(e, "amb_ensemble_run");
+    h->step += nsteps;
+    // finite check over every replica's current field
+    e = cudaMemsetAsync(h->d_flag, 0, sizeof(int), h->stream);
+    for (int r = 0; r < h->nrep && e == cudaSuccess; ++r)
+        e = amb::launch_nonfinite<float>(h->host_reps[r].phi[h->parity], size_t(h->ny[r]) * h->nx[r], h->d_flag,
+                                         h->stream);
+    int flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, h->d_flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return ecuda(e, "amb_ensemble_run");
+    if (flag) return efail(AMB_ERR_NONFINITE, "an unknown numerical error occurred during simulation");
+    return AMB_OK;
+}
+
+extern "C" int amb_ensemble_get_field(amb_ensemble* h, int replica, double* host_out)
+{
+    if (!h || !host_out || replica < 0 || replica >= h->nrep)
+        return efail(AMB_ERR_INVALID, "amb_ensemble_get_field: bad arguments");
+    const size_t n = size_t(h->ny[replica]) * h->nx[replica];
+    std::vector<float> tmp(n);
+    cudaError_t e = cudaMemcpyAsync(tmp.data(), h->host_reps[replica].phi[h->parity], n * sizeof(float),
+                                    cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return ecuda(e, "amb_ensemble_get_field");
+    for (size_t i = 0; i < n; ++i) host_out[i] = double(tmp[i]);
+    return AMB_OK;
+}
+
+extern "C" int amb_ensemble_info(const amb_ensemble* h, int64_t* timestep, int* ntasks, int* seg_rows)
+{
+    if (!h) return efail(AMB_ERR_INVALID, "NULL ensemble");
+    if (timestep) *timestep = h->step;
+    if (ntasks) *ntasks = h->ntasks;
+    if (seg_rows) *seg_rows = h->seg_h;
+    return AMB_OK;
+}

@@ -23,6 +23,27 @@ namespace amb
     bool step_f32_sliding_supported(int ny, int nx, int variant);
     int sliding_default_seg_h(int ny, int nx);
 
+    // ------------------------------------------------------------- ensemble
+    // One replica of a batched ensemble (device array of these, filled by the host).
+    struct EnsembleReplica
+    {
+        float* phi[2];               // ping-pong pair
+        __nv_bfloat16* residual;     // bf16 Kahan residual or nullptr
+        StepParams p;                // p.step unused: the launch reads the step from the device counter
+    };
+    // One warp-pair task: rows [r0, r1) of column strip `strip` of replica `replica`.
+    struct EnsembleTask
+    {
+        int replica, strip, r0, r1;
+    };
+    size_t sliding_coef_bytes();
+    void sliding_make_coef(const StepParams& p, void* out);  // host: per-replica coefficient block
+    int sliding_default_seg_h_for(int ny, int nx, int resident_pairs);
+    cudaError_t launch_sliding_ensemble(const EnsembleReplica* reps, const void* coefs, const EnsembleTask* tasks,
+                                        int ntasks, int parity, const int64_t* step_counter, int step_offset,
+                                        int comp_mode, int noise_mode, cudaStream_t stream);
+    cudaError_t ensemble_resident_pairs(int* out);
+
     template <typename Real>
     cudaError_t launch_terms(const Real* phi, double* out, const StepParams& p, int noise_mode, const Real* injected,
                              cudaStream_t stream);

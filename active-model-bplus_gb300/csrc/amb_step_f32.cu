@@ -18,12 +18,12 @@
 // The phi rows stream through a 16-row shared-memory ring filled by TMA bulk
 // copies (cp.async.bulk, completion on one mbarrier per ring slot) issued 8
 // rows ahead of use; a row window that crosses the periodic x boundary is
-// fetched as two aligned pieces. Every mbarrier wait is bounded: on timeout the
+// fetched as several aligned pieces. Every mbarrier wait is bounded: on timeout the
 // warp poisons its outputs with NaN (caught by the Integrator's finite check),
 // drains its own copies with a bounded wait, and leaves.
 //
 // Requirements (checked by step_f32_sliding_supported): ncols % 4 == 0 and
-// ncols >= 136 (a row window wraps at most once); any nrows >= 1.
+// ncols >= 112 (one strip's output width); any nrows >= 1.
 //
 // Arithmetic per site follows the same separable operators as the tile kernel
 // (amb_step_tile.cuh); the noise is the shared Philox definition (amb_common.cuh),
@@ -33,6 +33,7 @@
 #include "amb_step_tile.cuh"
 
 #include <cstdint>
+#include <cstring>
 
 namespace amb
 {
@@ -125,10 +126,15 @@ namespace amb
             int gr = wrap_index(t.r0 - 9 + m, ny);
             int gc = wrap_index(t.c0 - 12, nx);
             const float* row = phi + (size_t)gr * nx;
-            int n1 = nx - gc < kRowF ? nx - gc : kRowF;
             mbar_expect_tx(&sm.bar[slot], kRowBytes);
-            bulk_g2s(&sm.phi[slot][0], row + gc, uint32_t(n1) * 4u, &sm.bar[slot]);
-            if (n1 < kRowF) bulk_g2s(&sm.phi[slot][n1], row, uint32_t(kRowF - n1) * 4u, &sm.bar[slot]);
+            // the window is one aligned piece, or several where it wraps round a narrow grid
+            for (int dst = 0; dst < kRowF;)
+            {
+                int n = nx - gc < kRowF - dst ? nx - gc : kRowF - dst;
+                bulk_g2s(&sm.phi[slot][dst], row + gc, uint32_t(n) * 4u, &sm.bar[slot]);
+                dst += n;
+                gc = 0;
+            }
         }
 
         struct Coef
@@ -590,10 +596,43 @@ namespace amb
         }
     }
 
+    namespace sliding
+    {
+        // Batched form: one warp pair per task of a task table that spans many replicas of
+        // different sizes and parameters; the step index comes from device memory so that
+        // a captured CUDA graph of several steps can be replayed.
+        template <int COMP, int NOISE>
+        __global__ void __launch_bounds__(64)
+        sliding_ensemble_kernel(const EnsembleReplica* __restrict__ reps, const Coef* __restrict__ coefs,
+                                const EnsembleTask* __restrict__ tasks, int parity,
+                                const int64_t* __restrict__ step_counter, int step_offset)
+        {
+            extern __shared__ __align__(16) unsigned char smem_raw[];
+            const int role = (threadIdx.x >> 5) & 1, lane = threadIdx.x & 31;
+            PairSmem& sm = *reinterpret_cast<PairSmem*>(smem_raw);
+            const EnsembleTask bt = tasks[blockIdx.x];
+            const EnsembleReplica& rd = reps[bt.replica];
+            StepParams p = rd.p;
+            p.step = *step_counter + step_offset;
+            const Coef& k = coefs[bt.replica];
+            Task t;
+            int c0 = bt.strip * kOut;
+            t.store_lo = c0;
+            if (c0 + kOut > p.nx) c0 = p.nx - kOut;
+            t.c0 = c0;
+            t.r0 = bt.r0;
+            t.r1 = bt.r1;
+            if (role == 0)
+                producer<NOISE>(sm, rd.phi[parity], p, k, nullptr, t, lane, 1);
+            else
+                consumer<COMP, NOISE>(sm, rd.phi[parity ^ 1], rd.residual, p, k, nullptr, t, lane, 1);
+        }
+    }
+
     bool step_f32_sliding_supported(int ny, int nx, int variant)
     {
         (void)variant;
-        return ny >= 1 && nx >= 136 && nx % 4 == 0;
+        return ny >= 1 && nx >= sliding::kOut && nx % 4 == 0;
     }
 
     namespace
@@ -686,5 +725,74 @@ namespace amb
         if (wpb == 1) return by_noise<COMP_NONE, 1>(phi_in, phi_out, comp, p, noise_mode, injected, seg_h, stream);
         if (wpb == 3) return by_noise<COMP_NONE, 4>(phi_in, phi_out, comp, p, noise_mode, injected, seg_h, stream);
         return by_noise<COMP_NONE, 2>(phi_in, phi_out, comp, p, noise_mode, injected, seg_h, stream);
+    }
+}
+
+namespace amb
+{
+    size_t sliding_coef_bytes() { return sizeof(sliding::Coef); }
+
+    void sliding_make_coef(const StepParams& p, void* out)
+    {
+        sliding::Coef k(p);
+        std::memcpy(out, &k, sizeof(k));
+    }
+
+    int sliding_default_seg_h_for(int ny, int nx, int resident_pairs)
+    {
+        return choose_seg_h(ny, nx, resident_pairs);
+    }
+
+    namespace
+    {
+        template <int COMP, int NOISE>
+        cudaError_t launch_ensemble_variant(const EnsembleReplica* reps, const void* coefs, const EnsembleTask* tasks,
+                                            int ntasks, int parity, const int64_t* step_counter, int step_offset,
+                                            cudaStream_t stream)
+        {
+            using namespace sliding;
+            auto kern = sliding_ensemble_kernel<COMP, NOISE>;
+            static bool configured = false;
+            if (!configured)
+            {
+                cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     int(sizeof(PairSmem)));
+                if (e != cudaSuccess) return e;
+                configured = true;
+            }
+            kern<<<ntasks, 64, sizeof(PairSmem), stream>>>(reps, static_cast<const Coef*>(coefs), tasks, parity,
+                                                          step_counter, step_offset);
+            return cudaGetLastError();
+        }
+    }
+
+    cudaError_t ensemble_resident_pairs(int* out)
+    {
+        using namespace sliding;
+        auto kern = sliding_ensemble_kernel<COMP_BF16, NOISE_PHILOX>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(PairSmem)));
+        int dev = 0, sms = 0, blocks = 0;
+        if (e == cudaSuccess) e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, 64, sizeof(PairSmem));
+        if (e == cudaSuccess) *out = blocks * sms > 0 ? blocks * sms : 1;
+        return e;
+    }
+
+    cudaError_t launch_sliding_ensemble(const EnsembleReplica* reps, const void* coefs, const EnsembleTask* tasks,
+                                        int ntasks, int parity, const int64_t* step_counter, int step_offset,
+                                        int comp_mode, int noise_mode, cudaStream_t stream)
+    {
+        if (ntasks <= 0) return cudaSuccess;
+        const bool noise = noise_mode == NOISE_PHILOX;
+        if (comp_mode == COMP_BF16)
+            return noise ? launch_ensemble_variant<COMP_BF16, NOISE_PHILOX>(reps, coefs, tasks, ntasks, parity,
+                                                                            step_counter, step_offset, stream)
+                         : launch_ensemble_variant<COMP_BF16, NOISE_OFF>(reps, coefs, tasks, ntasks, parity,
+                                                                         step_counter, step_offset, stream);
+        return noise ? launch_ensemble_variant<COMP_NONE, NOISE_PHILOX>(reps, coefs, tasks, ntasks, parity, step_counter,
+                                                                        step_offset, stream)
+                     : launch_ensemble_variant<COMP_NONE, NOISE_OFF>(reps, coefs, tasks, ntasks, parity, step_counter,
+                                                                     step_offset, stream);
     }
 }

@@ -60,6 +60,8 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--temperature", type=float, default=0.05)
+    ap.add_argument("--ensemble", action="store_true",
+                    help="measure the batched ensemble workload (256 replicas of uneven sizes) instead")
     ap.add_argument("--launches", type=int, default=0,
                     help="profiling driver: run this many bare step launches through the C ABI and exit")
     return ap.parse_args()
@@ -393,6 +395,44 @@ def run_launches(args, w):
     print(json.dumps({"launches": args.launches, "size": w["ny"], "precision": args.precision}))
 
 
+def run_ensemble(args):
+    """Batched ensemble: 256 replicas, sizes drawn from {128,192,256,384,512,768,1024}^2, zeta in
+    [-4,4], lambda in [-1,1], phi0 in [-0.6,0.6], T in [0,0.1], a=-0.25 c=0.25 kappa=1, dt=1e-3,
+    f32c, numpy seed 7. One bench step = one Ensemble.run(inner) (one launch per time step over all
+    replicas, replayed from a captured CUDA graph)."""
+    import torch
+    from activemodelbplus.integrator import Ensemble, Model, Stencil
+    rng = np.random.default_rng(7)
+    sizes = rng.choice([128, 192, 256, 384, 512, 768, 1024], size=256)
+    fields, models = [], []
+    for n in sizes:
+        phi0 = rng.uniform(-0.6, 0.6)
+        fields.append(phi0 + 0.01 * rng.standard_normal((n, n)))
+        models.append(Model(-0.25, 0, 0.25, 1, rng.uniform(-1, 1), rng.uniform(-4, 4), rng.uniform(0, 0.1)))
+    sites = int(sum(int(n) * int(n) for n in sizes))
+    ens = Ensemble(fields, Stencil(1e-3, 1, 1), models, precision="f32c", seeds=list(range(256)), graph_steps=50)
+    flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        ens.run(args.inner)
+    torch.cuda.synchronize()
+    wall = 0.0
+    with ClockSampler(torch.cuda.current_device()) as clocks:
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ens.run(args.inner)
+            wall += time.perf_counter() - t0
+    value = args.steps * args.inner * sites / wall / 1e9
+    print(json.dumps({"metric": "ensemble Gsite-updates/s (256 replicas, uneven sizes)", "value": value, "unit": UNIT,
+                      "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True, "dtype": "f32",
+                      "data": "synthetic", "config": {"workload": "ensemble", "replicas": 256, "sites": sites,
+                                                      "inner_steps": args.inner, "tasks": ens.ntasks},
+                      "clocks": clocks.summary()}), flush=True)
+    ens.close()
+
+
 def main():
     args = parse_args()
     if args.warmup < 3:
@@ -402,6 +442,8 @@ def main():
     w = workload(args)
     if args.launches > 0:
         return run_launches(args, w)
+    if args.ensemble:
+        return run_ensemble(args)
     if args.impl == "reference":
         return run_reference_arm(args, w, rank, world)
     import torch

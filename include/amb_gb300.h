@@ -78,7 +78,7 @@ typedef struct amb_model
 /* Kernel selectors for amb_step_f32 (AMB_KERNEL_AUTO picks the fastest valid one). */
 #define AMB_KERNEL_AUTO 0
 #define AMB_KERNEL_TILE 1    /* shared-memory tile kernel, any grid */
-#define AMB_KERNEL_SLIDING 2 /* warp-pair sliding FP32 kernel (ncols % 4 == 0, ncols >= 136, 16-byte aligned) */
+#define AMB_KERNEL_SLIDING 2 /* warp-pair sliding FP32 kernel (ncols % 4 == 0, ncols >= 112, 16-byte aligned) */
 
 /* Explicit kernel configuration for amb_step_f32_ex (zeros mean defaults).
  * seg_rows: rows per warp-pair task of the sliding kernel; pairs_per_cta: 1, 2 or 4. */
@@ -187,6 +187,22 @@ int amb_mass_f32_noalloc(const float* field, int64_t n, double* out_sum, void* s
  * (src/integrator.cu:265-272). The caller zeroes the flag. */
 int amb_check_finite_f64(const double* field, int64_t n, int* flag, void* stream);
 int amb_check_finite_f32(const float* field, int64_t n, int* flag, void* stream);
+
+/* ================================================================ ensemble */
+/* No reference counterpart (the reference runs one integrator per process). Many
+ * independent replicas — any mix of sizes (ncols >= 112, ncols % 4 == 0) and model
+ * parameters, FP32 storage (AMB_F32 or AMB_F32C), one Philox seed each — advanced
+ * together: one launch per step covers every replica, and graph_steps (even; 0 = no
+ * graph) steps are captured once into a CUDA graph and replayed. */
+typedef struct amb_ensemble amb_ensemble;
+int amb_ensemble_create(int nreplicas, const int* nrows, const int* ncols, const double* const* host_fields,
+                        const amb_stencil* stencils, const amb_model* models, const uint64_t* seeds, int precision,
+                        int graph_steps, amb_ensemble** out);
+void amb_ensemble_destroy(amb_ensemble* h);
+/* Advance every replica nsteps steps, then check all fields are finite (AMB_ERR_NONFINITE). */
+int amb_ensemble_run(amb_ensemble* h, int nsteps);
+int amb_ensemble_get_field(amb_ensemble* h, int replica, double* host_out);
+int amb_ensemble_info(const amb_ensemble* h, int64_t* timestep, int* ntasks, int* seg_rows);
 
 /* ================================================================ analysis */
 

@@ -54,7 +54,7 @@ def initial(shape, seed=0):
     return -0.4 + 0.05 * rng.standard_normal(shape)
 
 
-@pytest.mark.parametrize("shape", [(256, 256), (200, 140), (37, 340), (17, 256), (96, 448), (5, 136)])
+@pytest.mark.parametrize("shape", [(256, 256), (200, 140), (37, 340), (17, 256), (96, 448), (5, 136), (128, 128), (40, 112), (64, 116)])
 @pytest.mark.parametrize("T", [0.0, 0.05])
 def test_sliding_matches_tile(shape, T):
     """Both FP32 kernels, 30 steps, plain FP32 and compensated: max |diff| < 2e-6
@@ -117,7 +117,7 @@ def test_sliding_rejects_unsupported_shapes():
     import torch
     N = native()
     p = Params(T=0.0, **AMB)
-    a = torch.zeros((32, 100), dtype=torch.float32, device="cuda")
+    a = torch.zeros((32, 100), dtype=torch.float32, device="cuda")  # ncols < 112
     b = torch.empty_like(a)
     s = N.amb_stencil(p.dt, p.dx, p.dy)
     m = N.amb_model(p.a, p.b, p.c, p.kappa, p.lamb, p.zeta, p.T)
