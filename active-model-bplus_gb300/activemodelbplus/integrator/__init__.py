@@ -15,7 +15,9 @@ Additions with no reference counterpart (all keyword-only or new names):
 ``precision`` ("f64" default, "f32", "f32c"), ``seed`` (Philox noise key; the
 reference seeds non-deterministically), ``kernel``, the chemical-potential
 getters the reference leaves unbound, ``mass()``, ``field_tensor``,
-``checkpoint()`` / ``Integrator.from_checkpoint()``, ``sample()``.
+``checkpoint()`` / ``Integrator.from_checkpoint()``, ``sample_trajectory()``
+(see ``activemodelbplus.trajectory`` for the ``.npz`` trajectory format),
+``Ensemble``.
 """
 from __future__ import annotations
 
@@ -265,7 +267,12 @@ class Integrator:
         longer finite. As in the reference, ``timestep`` advances by ``nsteps``
         even when ``nsteps <= 0``.
         """
-        nsteps = int(nsteps)
+        self._launch(int(nsteps))
+        self._check_finite()
+
+    def _launch(self, nsteps: int) -> None:
+        """Enqueue ``nsteps`` steps on the current stream and advance ``timestep``
+        (no host synchronisation)."""
         lib = N.lib()
         stream = self._stream()
         if nsteps > 0:
@@ -288,16 +295,24 @@ class Integrator:
             if in_spare.value:
                 self._cur = 1 - self._cur
         self._timestep += nsteps
-        self._check_finite()
 
-    def _check_finite(self) -> None:
+    def _enqueue_finite_check(self) -> None:
+        """OR a non-finite flag for the current field into ``self._flag`` (stream-ordered)."""
         lib = N.lib()
         f = self._buf[self._cur]
-        self._flag.zero_()
         fn = lib.amb_check_finite_f64 if self._precision == "f64" else lib.amb_check_finite_f32
         _check(fn(f.data_ptr(), f.numel(), self._flag.data_ptr(), self._stream()))
-        if int(self._flag.item()):
+
+    def _raise_if_flagged(self) -> None:
+        """Read the accumulated flag (one host synchronisation) and clear it."""
+        bad = int(self._flag.item())
+        self._flag.zero_()
+        if bad:
             raise CudaException("an unknown numerical error occurred during simulation")
+
+    def _check_finite(self) -> None:
+        self._enqueue_finite_check()
+        self._raise_if_flagged()
 
     # ------------------------------------------------------------- getters
     def _terms(self) -> np.ndarray:
@@ -446,11 +461,91 @@ class Integrator:
         d["model"] = tuple(d["model"].tolist())
         return cls.from_checkpoint(d, **kwargs)
 
+    # ---------------------------------------------------- trajectories
+    def sample_trajectory(self, t_samples, *, to: str = "host"):
+        """Run forward and record the field at each of ``t_samples`` (no reference
+        counterpart; it does what the analysis notebook does with ``run_for_time``
+        interrupts, examples/structureFactor.ipynb cell 1, without host round trips).
+
+        Args:
+            t_samples: non-decreasing times measured from the current time, each a
+                multiple of dt (0 records the current field).
+            to: "host" (float64 arrays, the ``.npz`` layout) or "device" (a device
+                tensor (n, ny, nx) of the storage dtype, e.g. for on-device S(k)).
+
+        The host waits once, at the end. Each sample is a device-to-device snapshot
+        taken on the compute stream; for ``to="host"`` the snapshot goes to pinned
+        memory on a copy stream that overlaps the next chunk of steps (two snapshot
+        buffers in rotation). The non-finite flag accumulates on the device and is
+        read once: :class:`CudaException` is raised at the end if any sample was
+        non-finite.
+
+        Returns:
+            :class:`activemodelbplus.trajectory.Trajectory`.
+        """
+        from ..trajectory import Trajectory
+
+        torch = _torch()
+        if to not in ("host", "device"):
+            raise ValueError('to must be "host" or "device"')
+        ts = np.atleast_1d(np.asarray(t_samples, dtype=np.float64))
+        steps = np.atleast_1d(steps_from_time(self._stencil.dt, ts)).astype(np.int64)
+        if steps.size == 0:
+            raise ValueError("no sample times given")
+        if np.any(steps < 0) or np.any(np.diff(steps) < 0):
+            raise ValueError("sample times must be non-negative and non-decreasing")
+        n = int(steps.size)
+        shape = (n, self._ny, self._nx)
+        dtype = self._buf[0].dtype
+        compute = torch.cuda.current_stream(self._device)
+        start = self._timestep
+        times = np.empty(n, dtype=np.float64)
+
+        if to == "device":
+            out = torch.empty(shape, dtype=dtype, device=self._device)
+            for i, st in enumerate(steps):
+                self._launch(int(start + st - self._timestep))
+                self._enqueue_finite_check()
+                out[i].copy_(self._buf[self._cur])
+                times[i] = self.time
+            self._raise_if_flagged()
+            return Trajectory(times, out, self.model, self.stencil)
+
+        host = torch.empty(shape, dtype=dtype, pin_memory=True)
+        nstage = min(2, n)
+        stage = [torch.empty((self._ny, self._nx), dtype=dtype, device=self._device) for _ in range(nstage)]
+        drained = [None] * nstage  # copy-stream event: the D2H out of stage[k] has finished
+        copier = torch.cuda.Stream(self._device)
+        for i, st in enumerate(steps):
+            self._launch(int(start + st - self._timestep))
+            self._enqueue_finite_check()
+            k = i % nstage
+            if drained[k] is not None:
+                compute.wait_event(drained[k])
+            stage[k].copy_(self._buf[self._cur])
+            ready = torch.cuda.Event()
+            ready.record(compute)
+            copier.wait_event(ready)
+            with torch.cuda.stream(copier):
+                host[i].copy_(stage[k], non_blocking=True)
+                done = torch.cuda.Event()
+                done.record(copier)
+            drained[k] = done
+            times[i] = self.time
+        copier.synchronize()
+        self._raise_if_flagged()
+        return Trajectory(times, host.numpy().astype(np.float64), self.model, self.stencil)
+
     # ---------------------------------------------------- run_for_time
     def run_for_time(self, t, show_progress=False, t_interrupt=None, f_interrupt=None,
                      max_updates=100, min_update_time=10):
         """Run for simulation time ``t`` in chunks, calling ``f_interrupt(self)`` at
         ``t_interrupt`` (activemodelbplus/integrator/__init__.py:105-161).
+
+        Chunks are enqueued without a host wait between them; a non-finite field
+        raises :class:`CudaException` at the next interrupt or at the end, where the
+        reference raises after the chunk. For sampling without host round trips use
+        :meth:`sample_trajectory`.
 
         Raises:
             ValueError: if ``t`` or an interrupt time is not a multiple of dt.
@@ -477,14 +572,19 @@ class Integrator:
                 for out in (sys.stdout, sys.stderr):
                     out.flush()
             if t_interrupt is not None and np.any(np.isclose(self.time - initial_time, t_interrupt)):
+                self._raise_if_flagged()
                 f_interrupt(self)
             assert n > 0
-            self.run(n)
+            # chunks are enqueued without waiting; the non-finite flag is read at
+            # the next interrupt or at the end
+            self._launch(int(n))
+            self._enqueue_finite_check()
             if plot is not None:
                 plot.update(self.field)
 
         if plot is not None:
             plot.close()
+        self._raise_if_flagged()
         assert (self.timestep - initial_timestep) == nsteps
         if t_interrupt is not None and np.any(np.isclose(self.time - initial_time, t_interrupt)):
             f_interrupt(self)
@@ -540,6 +640,33 @@ class Ensemble:
     @property
     def fields(self):
         return [self.field(r) for r in range(len(self._shapes))]
+
+    @property
+    def offsets(self) -> np.ndarray:
+        """Start of each replica in the packed layout of :meth:`gather` (length n + 1)."""
+        return np.concatenate([[0], np.cumsum([r * c for r, c in self._shapes])]).astype(np.int64)
+
+    def gather(self, out=None):
+        """Every replica's current field packed back to back in one FP32 device tensor
+        (device-to-device; replica r at ``offsets[r]``)."""
+        torch = _torch()
+        n = int(self.offsets[-1])
+        if out is None:
+            out = torch.empty(n, dtype=torch.float32, device="cuda")
+        if out.dtype != torch.float32 or out.numel() < n or not out.is_contiguous():
+            raise ValueError("out must be a contiguous float32 device tensor with room for every replica")
+        torch.cuda.current_stream().synchronize()
+        _check(N.lib().amb_ensemble_gather(self._h, out.data_ptr()))
+        return out
+
+    def scatter(self, src) -> None:
+        """Set every replica's field from a packed FP32 device tensor (the layout of
+        :meth:`gather`); clears the compensation residuals."""
+        torch = _torch()
+        if src.dtype != torch.float32 or src.numel() < int(self.offsets[-1]) or not src.is_contiguous():
+            raise ValueError("src must be a contiguous float32 device tensor in the packed layout")
+        torch.cuda.current_stream().synchronize()
+        _check(N.lib().amb_ensemble_scatter(self._h, src.data_ptr()))
 
     def _info(self):
         ts, nt, sr = ctypes.c_int64(), ctypes.c_int(), ctypes.c_int()

@@ -283,3 +283,39 @@ extern "C" int amb_ensemble_info(const amb_ensemble* h, int64_t* timestep, int* 
     if (seg_rows) *seg_rows = h->seg_h;
     return AMB_OK;
 }
+
+// Device-to-device copies of every replica's current field, packed back to back in
+// replica order (replica r at offset sum_{q<r} nrows_q * ncols_q). Synchronous.
+extern "C" int amb_ensemble_gather(amb_ensemble* h, float* dst)
+{
+    if (!h || !dst) return efail(AMB_ERR_INVALID, "amb_ensemble_gather: bad arguments");
+    cudaError_t e = cudaSuccess;
+    size_t off = 0;
+    for (int r = 0; r < h->nrep && e == cudaSuccess; ++r)
+    {
+        const size_t n = size_t(h->ny[r]) * h->nx[r];
+        e = cudaMemcpyAsync(dst + off, h->host_reps[r].phi[h->parity], n * sizeof(float), cudaMemcpyDeviceToDevice,
+                            h->stream);
+        off += n;
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? AMB_OK : ecuda(e, "amb_ensemble_gather");
+}
+
+extern "C" int amb_ensemble_scatter(amb_ensemble* h, const float* src)
+{
+    if (!h || !src) return efail(AMB_ERR_INVALID, "amb_ensemble_scatter: bad arguments");
+    cudaError_t e = cudaSuccess;
+    size_t off = 0;
+    for (int r = 0; r < h->nrep && e == cudaSuccess; ++r)
+    {
+        const size_t n = size_t(h->ny[r]) * h->nx[r];
+        e = cudaMemcpyAsync(h->host_reps[r].phi[h->parity], src + off, n * sizeof(float), cudaMemcpyDeviceToDevice,
+                            h->stream);
+        if (e == cudaSuccess && h->host_reps[r].residual)
+            e = cudaMemsetAsync(h->host_reps[r].residual, 0, n * sizeof(__nv_bfloat16), h->stream);
+        off += n;
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? AMB_OK : ecuda(e, "amb_ensemble_scatter");
+}

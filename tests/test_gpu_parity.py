@@ -398,3 +398,53 @@ def test_run_for_time_with_interrupts():
     assert seen == [0, 25, 50, 100]
     with pytest.raises(ValueError):
         sim.run_for_time(0.015)
+
+
+# ------------------------------------------------------------------ trajectories
+
+@pytest.mark.parametrize("precision", ["f64", "f32c"])
+@pytest.mark.parametrize("to", ["host", "device"])
+def test_sample_trajectory_matches_chunked_runs(precision, to, tmp_path):
+    """sample_trajectory (no host wait between samples) records exactly the fields
+    that run() in the same chunks produces; the file reloads unchanged."""
+    I = lib_integrator()
+    from activemodelbplus.trajectory import Trajectory
+    f0 = -0.4 + 0.01 * np.random.default_rng(4).standard_normal((64, 128))
+    st, mo = I.Stencil(1e-3, 1, 1), I.Model(-0.25, 0, 0.25, 1, -1, -4, 0.05)
+    t = np.array([0.0, 0.005, 0.005, 0.02, 0.1])
+    a = I.Integrator(f0, st, mo, precision=precision, seed=5)
+    a.run(10)
+    tr = a.sample_trajectory(t, to=to)
+    b = I.Integrator(f0, st, mo, precision=precision, seed=5)
+    b.run(10)
+    expect = []
+    for n in np.round(t / 1e-3).astype(int):
+        b.run(int(n + 10 - b.timestep))
+        expect.append(b.field)
+    assert a.timestep == 110
+    assert np.allclose(tr.time, 0.01 + t)
+    assert np.array_equal(tr.host_field(), np.asarray(expect))
+    tr.save(str(tmp_path / "trajectory.npz"))
+    back = Trajectory.load(str(tmp_path / "trajectory.npz"))
+    assert np.array_equal(back.field, tr.host_field()) and back.model == mo and back.stencil == st
+
+
+def test_sample_trajectory_rejects_and_raises():
+    I = lib_integrator()
+    sim = I.Integrator(np.zeros((32, 32)), I.Stencil(1e-2, 1, 1), I.Model(-0.25, 0, 0.25, 1, 0, 0, 0))
+    with pytest.raises(ValueError):
+        sim.sample_trajectory([0.1, 0.05])
+    with pytest.raises(ValueError):
+        sim.sample_trajectory([0.015])
+    blow = I.Integrator(np.random.default_rng(0).uniform(-1, 1, (32, 32)), I.Stencil(10.0, 1, 1),
+                        I.Model(-0.25, 0, 0.25, 1, 0, 0, 0), precision="f32c")
+    with pytest.raises(I.CudaException):
+        blow.sample_trajectory([10.0, 500.0])
+
+
+def test_run_for_time_raises_on_nonfinite():
+    I = lib_integrator()
+    blow = I.Integrator(np.random.default_rng(0).uniform(-1, 1, (32, 32)), I.Stencil(10.0, 1, 1),
+                        I.Model(-0.25, 0, 0.25, 1, 0, 0, 0), precision="f32c")
+    with pytest.raises(I.CudaException):
+        blow.run_for_time(500.0, max_updates=5, min_update_time=10.0)
