@@ -22,6 +22,7 @@ AMB_ERR_UNSUPPORTED = 5
 AMB_F64, AMB_F32, AMB_F32C = 0, 1, 2
 AMB_KERNEL_AUTO, AMB_KERNEL_TILE, AMB_KERNEL_SLIDING = 0, 1, 2
 AMB_NTERMS = 10
+AMB_EPI_GELU, AMB_EPI_F32, AMB_EPI_GELU_BWD = 0, 1, 2
 CURRENTS = {"total": 0, "deterministic": 1, "passive": 2, "active": 3, "lambda": 4, "circulating": 5, "random": 6}
 MUS = {"total": 0, "passive": 1, "active": 2}
 
@@ -85,6 +86,15 @@ SIGNATURES = {
     "amb_label_components_f32": (_I, [_VP, _I, _I, ctypes.c_double, _VP, _VP, _VP]),
     "amb_check_finite_f64": (_I, [_VP, _I64, _VP, _VP]),
     "amb_check_finite_f32": (_I, [_VP, _I64, _VP, _VP]),
+    "amb_ensemble_gather": (_I, [_VP, _VP]),
+    "amb_ensemble_scatter": (_I, [_VP, _VP]),
+    "amb_tc_selftest": (_I, [_VP, _VP, _VP, _I, _I, _I, _I, _VP, _VP]),
+    "amb_conv5x5_forward": (_I, [_VP, _I, _I, _I, _I, _VP, _VP, _I, _I, _I, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "amb_conv5x5_wgrad_scratch_bytes": (ctypes.c_size_t, [_I, _I, _I, _I, _I]),
+    "amb_conv5x5_wgrad": (_I, [_VP, _VP, _I, _I, _I, _I, _I, _VP, _VP, ctypes.c_size_t, _VP, _VP]),
+    "amb_learned_input": (_I, [_VP, _VP, _I, _I, _I, _VP, _VP]),
+    "amb_learned_update": (_I, [_VP, _I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                _U64, _VP, _VP, _VP, _VP, ctypes.c_double, _VP, _VP]),
 }
 
 _lib = None

@@ -1,0 +1,938 @@
+// Learned coarse stepper kernels (no reference counterpart): 5x5 circular
+// convolutions as BF16 implicit GEMMs on the tcgen05 tensor cores with FP32
+// accumulation in TMEM, for both inference and training, plus the
+// mass-conserving fixed-point update that applies the predicted flux.
+//
+// Activation layout ("chunk planes"): bf16 [batch][C/8][nrows][ncols][8], i.e.
+// for each group of 8 channels a plane of 16-byte sites. One 16-byte site row
+// is one row of a tensor-core core matrix, so a tap shift of one site along x
+// is a 16-byte move of the operand start address.
+//
+// Forward / data-gradient kernel (conv_fwd_kernel): one CTA owns a 128-site
+// window of a row range. GEMM per output row: M = 128 sites, N = Cout (16 or
+// 32), K = 25 taps x Cin, issued as 25 x Cin/16 MMAs of 128 x N x 16 with the A
+// operand read straight from the staged input rows (K-major, LBO = one channel
+// chunk plane, SBO = 8 sites). Warp 0 stages input rows into a ring with bulk
+// copies (periodic wrap in both axes), warp 1 issues the MMAs into one of two
+// TMEM accumulators, warps 2-5 run the epilogue (bias, GELU, its derivative, or
+// FP32 output) and store. The data gradient of a circular convolution is the
+// forward convolution with the kernel flipped and the channel roles swapped, so
+// the same kernel serves it with the GELU-derivative epilogue.
+//
+// Weight-gradient kernel (conv_wgrad_kernel): dW[tap][ci][co] = sum over sites
+// of X[ci][site + tap] dZ[co][site]. Per MMA: M = 128 rows = (ky block, ci), with
+// 16/(Cin/8) ky values stacked along M (the staged rows sit at a uniform pitch,
+// so (ky, chunk) is one uniform M stride), N = Cout, K = 16 sites; both operands
+// MN-major. Partial sums per CTA go to scratch and a second kernel reduces them
+// in a fixed order (deterministic gradients).
+#include "amb_gb300.h"
+#include "amb_kernels.h"
+#include "amb_tc.cuh"
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+#include <string>
+
+namespace
+{
+    using namespace amb::tc;
+
+    constexpr int kTile = 128;              // output sites per tile (one row window)
+    constexpr int kSites = kTile + 4;       // staged input sites per row (halo 2 on each side)
+    constexpr int kRowPlane = kSites * 16;  // bytes of one channel chunk of one staged row
+    constexpr int kRing = 6;                // staged input rows (forward kernel)
+    constexpr int kThreads = 192;           // warp 0 loads, warp 1 issues MMAs, warps 2-5 epilogue
+    constexpr int kTaps = 25;
+
+    enum Epilogue
+    {
+        EPI_GELU = 0,      // out = bf16(gelu(acc + bias)), pre = bf16(acc + bias)
+        EPI_F32 = 1,       // out_f32 = acc + bias (first `cout` channels)
+        EPI_GELU_BWD = 2,  // out = bf16(acc * gelu'(gate))
+    };
+
+    struct FwdArgs
+    {
+        const uint16_t* in;     // [batch][cin/8][nrows][ncols][8]
+        const uint16_t* wimg;   // [25][cin/8][npad][8] (B operand image, K-major)
+        const float* bias;      // [npad] or null
+        uint16_t* out;          // [batch][npad/8][nrows][ncols][8]
+        uint16_t* pre;          // optional, same layout as out
+        const uint16_t* gate;   // EPI_GELU_BWD: same layout as out
+        float* out_f32;         // [batch][cout][nrows][ncols]
+        int batch, nrows, ncols, cin_chunks, npad, cout, epilogue, rows_per_cta;
+        int* error;
+    };
+
+    struct WgradArgs
+    {
+        const uint16_t* x;   // [batch][cin/8][nrows][ncols][8]
+        const uint16_t* dz;  // [batch][npad/8][nrows][ncols][8]
+        float* partial;      // [grid][25][cin][npad]
+        int batch, nrows, ncols, cin_chunks, npad, rows_per_cta;
+        int* error;
+    };
+
+    __host__ __device__ constexpr uint32_t align128(uint32_t x) { return (x + 127u) & ~127u; }
+
+    __host__ __device__ inline uint32_t fwd_weight_bytes(int cc, int npad) { return uint32_t(kTaps) * cc * npad * 16u; }
+    __host__ __device__ inline uint32_t fwd_ring_offset(int cc, int npad) { return align128(fwd_weight_bytes(cc, npad)); }
+    __host__ __device__ inline uint32_t fwd_bar_offset(int cc, int npad)
+    {
+        return fwd_ring_offset(cc, npad) + uint32_t(kRing) * cc * kRowPlane;
+    }
+    __host__ __device__ inline uint32_t fwd_smem_bytes(int cc, int npad) { return fwd_bar_offset(cc, npad) + 256u; }
+
+    // wgrad: ky blocks per MMA along M, staged X rows per output-row range
+    __host__ __device__ inline int wg_kb(int cc) { return 16 / cc; }
+    __host__ __device__ inline int wg_nstarts(int cc) { return wg_kb(cc) >= 5 ? 1 : 2; }
+    __host__ __device__ inline int wg_start(int cc, int si) { return si == 0 ? 0 : 5 - wg_kb(cc); }
+    __host__ __device__ inline int wg_extra_rows(int cc) { return wg_kb(cc) - 1 > 4 ? wg_kb(cc) - 1 : 4; }
+    __host__ __device__ inline uint32_t wg_x_bytes(int cc, int rows) { return uint32_t(rows + wg_extra_rows(cc)) * cc * kRowPlane; }
+    __host__ __device__ inline uint32_t wg_dz_bytes(int npad, int rows) { return uint32_t(rows) * (npad / 8) * kTile * 16u; }
+    __host__ __device__ inline uint32_t wg_bar_offset(int cc, int npad, int rows)
+    {
+        return align128(wg_x_bytes(cc, rows)) + align128(wg_dz_bytes(npad, rows));
+    }
+    constexpr uint32_t kWgradMinSmem = 120u * 1024u;  // keeps one wgrad CTA per SM (it owns all of TMEM)
+    __host__ __device__ inline uint32_t wg_smem_bytes(int cc, int npad, int rows)
+    {
+        uint32_t need = wg_bar_offset(cc, npad, rows) + 256u;
+        return need > kWgradMinSmem ? need : kWgradMinSmem;
+    }
+
+    __device__ __forceinline__ void give_up(int* error, volatile int* abort, int code)
+    {
+        *abort = 1;
+        if (error) atomicExch(error, code);
+    }
+
+    __device__ __forceinline__ int wrap_row(int r, int n)
+    {
+        r %= n;
+        return r < 0 ? r + n : r;
+    }
+
+    __device__ __forceinline__ float gelu_f(float z)
+    {
+        return 0.5f * z * (1.f + erff(z * 0.70710678118654752f));
+    }
+
+    __device__ __forceinline__ float gelu_grad_f(float z)
+    {
+        return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * __expf(-0.5f * z * z);
+    }
+
+    __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
+    {
+        __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+        return *reinterpret_cast<uint32_t*>(&h);
+    }
+
+    __device__ __forceinline__ void unpack_bf16x8(const uint4& u, float (&f)[8])
+    {
+        const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+        {
+            f[2 * i] = __uint_as_float(w[i] << 16);
+            f[2 * i + 1] = __uint_as_float(w[i] & 0xFFFF0000u);
+        }
+    }
+
+    // ================================================================ self-test
+    // One CTA: D (128 x n) = A (128 x k) * B (n x k)^T from row-major inputs, with A
+    // and B staged in the K-major or MN-major core-matrix layout. Layout constants:
+    //   K-major  A: SBO = 128 (8-row groups along M), LBO = 16 * 128 (K chunks)
+    //   MN-major A: LBO = 128 (8-row K groups),       SBO = (k / 8) * 128 (M groups)
+    //   (B likewise with n in place of 128.)
+    __global__ void __launch_bounds__(128) tc_selftest_kernel(const uint16_t* __restrict__ A,
+                                                              const uint16_t* __restrict__ B, float* __restrict__ D,
+                                                              int n, int k, int a_mn, int b_mn, int* error)
+    {
+        extern __shared__ __align__(1024) uint8_t smem[];
+        uint8_t* sa = smem;             // 64 KB region (A uses at most 16 KB)
+        uint8_t* sb = smem + 65536;     // 32 KB region (B uses at most 4 KB)
+        uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 98304);
+        uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + 98304 + 64);
+        volatile int* abort = reinterpret_cast<volatile int*>(smem + 98304 + 128);
+        const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+        // zero both regions, then scatter the operands
+        for (int i = tid; i < 98304 / 16; i += 128) reinterpret_cast<uint4*>(smem)[i] = make_uint4(0, 0, 0, 0);
+        __syncthreads();
+        for (int idx = tid; idx < 128 * k; idx += 128)
+        {
+            int m = idx / k, kk = idx % k;
+            uint32_t off = a_mn ? (m / 8) * (k / 8) * 128 + (kk / 8) * 128 + (kk % 8) * 16 + (m % 8) * 2
+                                : (kk / 8) * 16 * 128 + (m / 8) * 128 + (m % 8) * 16 + (kk % 8) * 2;
+            *reinterpret_cast<uint16_t*>(sa + off) = A[idx];
+        }
+        for (int idx = tid; idx < n * k; idx += 128)
+        {
+            int r = idx / k, kk = idx % k;
+            uint32_t off = b_mn ? (r / 8) * (k / 8) * 128 + (kk / 8) * 128 + (kk % 8) * 16 + (r % 8) * 2
+                                : (kk / 8) * (n / 8) * 128 + (r / 8) * 128 + (r % 8) * 16 + (kk % 8) * 2;
+            *reinterpret_cast<uint16_t*>(sb + off) = B[idx];
+        }
+        if (tid == 0)
+        {
+            mbar_init(bar, 1);
+            *abort = 0;
+            fence_mbar_init();
+        }
+        fence_proxy_async();
+        if (warp == 0)
+        {
+            tmem_alloc(tslot, 32);
+            tmem_relinquish();
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        const uint32_t tbase = *tslot;
+
+        if (tid == 0)
+        {
+            const uint32_t idesc = idesc_bf16(128, n, a_mn != 0, b_mn != 0);
+            const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+            for (int ks = 0; ks < k / 16; ++ks)
+            {
+                uint64_t ad = a_mn ? smem_desc(a0 + 2 * ks * 128, 128, (k / 8) * 128)
+                                   : smem_desc(a0 + 2 * ks * 16 * 128, 16 * 128, 128);
+                uint64_t bd = b_mn ? smem_desc(b0 + 2 * ks * 128, 128, (k / 8) * 128)
+                                   : smem_desc(b0 + 2 * ks * (n / 8) * 128, (n / 8) * 128, 128);
+                mma_bf16(tbase, ad, bd, idesc, ks > 0 ? 1u : 0u);
+            }
+            mma_commit(bar);
+        }
+        bool ok = mbar_wait(bar, 0, nullptr);
+        ok = __all_sync(0xffffffffu, ok);
+        if (ok)
+        {
+            tc_fence_after();
+            float v[32];
+            const uint32_t taddr = tbase + (uint32_t(warp * 32) << 16);
+            if (n == 32) tmem_ld32(taddr, v);
+            else tmem_ld16(taddr, v);
+            tmem_wait_ld();
+            const int m = warp * 32 + lane;
+#pragma unroll
+            for (int c = 0; c < 32; ++c)
+                if (c < n) D[m * n + c] = v[c];
+        }
+        else if (lane == 0)
+            give_up(error, abort, 1);
+        tc_fence_before();
+        __syncthreads();
+        if (warp == 0)
+        {
+            tc_fence_after();
+            tmem_dealloc(tbase, 32);
+        }
+    }
+
+    // ============================================================== forward
+    __global__ void __launch_bounds__(kThreads) conv_fwd_kernel(const FwdArgs a)
+    {
+        extern __shared__ __align__(1024) uint8_t smem[];
+        const int cc = a.cin_chunks, npad = a.npad;
+        const uint32_t wbytes = fwd_weight_bytes(cc, npad);
+        const uint32_t slot_bytes = uint32_t(cc) * kRowPlane;
+        uint8_t* wsm = smem;
+        uint8_t* ring = smem + fwd_ring_offset(cc, npad);
+        uint64_t* bars = reinterpret_cast<uint64_t*>(smem + fwd_bar_offset(cc, npad));
+        uint64_t* full = bars;
+        uint64_t* empty = bars + kRing;
+        uint64_t* accf = bars + 2 * kRing;
+        uint64_t* acce = accf + 2;
+        uint64_t* wbar = acce + 2;
+        uint64_t* done = wbar + 1;
+        uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+        volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
+
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const int nwin = a.ncols / kTile;
+        const int ngroups = (a.nrows + a.rows_per_cta - 1) / a.rows_per_cta;
+        int t = blockIdx.x;
+        const int cw = t % nwin;
+        t /= nwin;
+        const int rg = t % ngroups;
+        const int b = t / ngroups;
+        const int c0 = cw * kTile;
+        const int r0 = rg * a.rows_per_cta;
+        const int nout = min(a.rows_per_cta, a.nrows - r0);
+        const int nin = nout + 4;
+
+        if (threadIdx.x == 0)
+        {
+            for (int i = 0; i < kRing; ++i)
+            {
+                mbar_init(&full[i], 1);
+                mbar_init(&empty[i], 1);
+            }
+            for (int i = 0; i < 2; ++i)
+            {
+                mbar_init(&accf[i], 1);
+                mbar_init(&acce[i], 128);
+            }
+            mbar_init(wbar, 1);
+            mbar_init(done, 1);
+            *abort = 0;
+            fence_mbar_init();
+        }
+        if (warp == 0)
+        {
+            tmem_alloc(tslot, 64);
+            tmem_relinquish();
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        const uint32_t tbase = *tslot;
+
+        if (warp == 0)
+        {
+            if (lane == 0)
+            {
+                mbar_expect_tx(wbar, wbytes);
+                bulk_g2s(wsm, a.wimg, wbytes, wbar);
+                int issued = 0;
+                const int cl = (c0 - 2 + a.ncols) % a.ncols;
+                const int cr = (c0 + kTile) % a.ncols;
+                for (int i = 0; i < nin; ++i)
+                {
+                    const int s = i % kRing;
+                    if (i >= kRing && !mbar_wait(&empty[s], ((i / kRing) - 1) & 1, abort))
+                    {
+                        give_up(a.error, abort, 1);
+                        break;
+                    }
+                    const int row = wrap_row(r0 - 2 + i, a.nrows);
+                    mbar_expect_tx(&full[s], slot_bytes);
+                    uint8_t* dst = ring + s * slot_bytes;
+                    for (int q = 0; q < cc; ++q)
+                    {
+                        const uint16_t* src = a.in + (size_t(b * cc + q) * a.nrows + row) * size_t(a.ncols) * 8;
+                        uint8_t* d = dst + q * kRowPlane;
+                        bulk_g2s(d, src + size_t(cl) * 8, 32, &full[s]);
+                        bulk_g2s(d + 32, src + size_t(c0) * 8, kTile * 16, &full[s]);
+                        bulk_g2s(d + 32 + kTile * 16, src + size_t(cr) * 8, 32, &full[s]);
+                    }
+                    issued = i + 1;
+                }
+                // no copy may still be in flight when the CTA exits
+                mbar_wait(wbar, 0, nullptr);
+                for (int i = issued > kRing ? issued - kRing : 0; i < issued; ++i)
+                    mbar_wait(&full[i % kRing], (i / kRing) & 1, nullptr);
+            }
+        }
+        else if (warp == 1)
+        {
+            if (lane == 0)
+            {
+                const uint32_t idesc = idesc_bf16(128, npad, false, false);
+                const uint32_t wsa = smem_u32(wsm), rsa = smem_u32(ring);
+                bool ok = mbar_wait(wbar, 0, abort);
+                bool issued_any = false;
+                for (int j = 0; ok && j < nout; ++j)
+                {
+                    const int acc = j & 1;
+                    if (j >= 2 && !mbar_wait(&acce[acc], ((j >> 1) - 1) & 1, abort))
+                    {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t d = tbase + uint32_t(acc * npad);
+                    uint32_t accumulate = 0;
+                    for (int ky = 0; ky < 5 && ok; ++ky)
+                    {
+                        const int i = j + ky, s = i % kRing;
+                        if (!mbar_wait(&full[s], (i / kRing) & 1, abort))
+                        {
+                            ok = false;
+                            break;
+                        }
+                        const uint32_t sa = rsa + s * slot_bytes;
+                        for (int kx = 0; kx < 5; ++kx)
+                            for (int ks = 0; ks < cc / 2; ++ks)
+                            {
+                                const uint64_t ad = smem_desc(sa + 2 * ks * kRowPlane + kx * 16, kRowPlane, 128);
+                                const uint64_t bd =
+                                    smem_desc(wsa + ((ky * 5 + kx) * cc + 2 * ks) * npad * 16, npad * 16, 128);
+                                mma_bf16(d, ad, bd, idesc, accumulate);
+                                accumulate = 1;
+                                issued_any = true;
+                            }
+                    }
+                    if (!ok) break;
+                    mma_commit(&accf[acc]);
+                    mma_commit(&empty[j % kRing]);
+                }
+                if (!ok) give_up(a.error, abort, 2);
+                if (issued_any)
+                {
+                    mma_commit(done);
+                    mbar_wait(done, 0, nullptr);
+                }
+            }
+        }
+        else
+        {
+            const int q4 = warp & 3;  // the TMEM lane quarter this warp may read
+            const int m = q4 * 32 + lane;
+            const int col = c0 + m;
+            const int nq = npad / 8;
+            for (int j = 0; j < nout; ++j)
+            {
+                const int acc = j & 1;
+                bool ok = mbar_wait(&accf[acc], (j >> 1) & 1, abort);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok)
+                {
+                    if (lane == 0) give_up(a.error, abort, 3);
+                    break;
+                }
+                tc_fence_after();
+                float v[32];
+                const uint32_t taddr = tbase + (uint32_t(q4 * 32) << 16) + uint32_t(acc * npad);
+                if (npad == 32) tmem_ld32(taddr, v);
+                else tmem_ld16(taddr, v);
+                tmem_wait_ld();
+                tc_fence_before();
+                mbar_arrive(&acce[acc]);
+
+                const int row = r0 + j;
+                const size_t site = size_t(row) * a.ncols + col;
+                const size_t plane = size_t(a.nrows) * a.ncols;
+                if (a.epilogue == EPI_F32)
+                {
+#pragma unroll
+                    for (int n = 0; n < 32; ++n)
+                        if (n < a.cout)
+                            a.out_f32[(size_t(b) * a.cout + n) * plane + site] = v[n] + (a.bias ? a.bias[n] : 0.f);
+                }
+                else
+                {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                    {
+                        if (q >= nq) break;
+                        const size_t off = ((size_t(b) * nq + q) * plane + site) * 8;
+                        float o[8];
+                        if (a.epilogue == EPI_GELU)
+                        {
+                            float z[8];
+#pragma unroll
+                            for (int e = 0; e < 8; ++e)
+                            {
+                                z[e] = v[8 * q + e] + (a.bias ? a.bias[8 * q + e] : 0.f);
+                                o[e] = gelu_f(z[e]);
+                            }
+                            if (a.pre)
+                                *reinterpret_cast<uint4*>(a.pre + off) =
+                                    make_uint4(pack_bf16x2(z[0], z[1]), pack_bf16x2(z[2], z[3]),
+                                               pack_bf16x2(z[4], z[5]), pack_bf16x2(z[6], z[7]));
+                        }
+                        else
+                        {
+                            float g[8];
+                            unpack_bf16x8(*reinterpret_cast<const uint4*>(a.gate + off), g);
+#pragma unroll
+                            for (int e = 0; e < 8; ++e) o[e] = v[8 * q + e] * gelu_grad_f(g[e]);
+                        }
+                        *reinterpret_cast<uint4*>(a.out + off) =
+                            make_uint4(pack_bf16x2(o[0], o[1]), pack_bf16x2(o[2], o[3]), pack_bf16x2(o[4], o[5]),
+                                       pack_bf16x2(o[6], o[7]));
+                    }
+                }
+            }
+        }
+
+        tc_fence_before();
+        __syncthreads();
+        if (warp == 0)
+        {
+            tc_fence_after();
+            tmem_dealloc(tbase, 64);
+        }
+    }
+
+    // =========================================================== weight grad
+    __global__ void __launch_bounds__(kThreads) conv_wgrad_kernel(const WgradArgs a)
+    {
+        extern __shared__ __align__(1024) uint8_t smem[];
+        const int cc = a.cin_chunks, npad = a.npad, nq = npad / 8;
+        const int R = a.rows_per_cta;
+        const uint32_t xrow = uint32_t(cc) * kRowPlane;    // bytes per staged X row
+        const uint32_t dzrow = uint32_t(nq) * kTile * 16;  // bytes per staged dZ row
+        uint8_t* xs = smem;
+        uint8_t* dzs = smem + align128(wg_x_bytes(cc, R));
+        uint64_t* bars = reinterpret_cast<uint64_t*>(smem + wg_bar_offset(cc, npad, R));
+        uint64_t* ld = bars;
+        uint64_t* done = bars + 1;
+        uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
+        volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
+
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const int nwin = a.ncols / kTile;
+        const int ngroups = (a.nrows + R - 1) / R;
+        int t = blockIdx.x;
+        const int cw = t % nwin;
+        t /= nwin;
+        const int rg = t % ngroups;
+        const int b = t / ngroups;
+        const int c0 = cw * kTile;
+        const int r0 = rg * R;
+        const int nout = min(R, a.nrows - r0);
+        const int nx_rows = nout + wg_extra_rows(cc);
+        const int kb = wg_kb(cc), nst = wg_nstarts(cc);
+
+        if (threadIdx.x == 0)
+        {
+            mbar_init(ld, 1);
+            mbar_init(done, 1);
+            *abort = 0;
+            fence_mbar_init();
+        }
+        if (warp == 0)
+        {
+            tmem_alloc(tslot, 512);
+            tmem_relinquish();
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        const uint32_t tbase = *tslot;
+
+        if (warp == 0)
+        {
+            if (lane == 0)
+            {
+                const uint32_t bytes = uint32_t(nx_rows) * xrow + uint32_t(nout) * dzrow;
+                mbar_expect_tx(ld, bytes);
+                const int cl = (c0 - 2 + a.ncols) % a.ncols;
+                const int cr = (c0 + kTile) % a.ncols;
+                for (int i = 0; i < nx_rows; ++i)
+                {
+                    const int row = wrap_row(r0 - 2 + i, a.nrows);
+                    for (int q = 0; q < cc; ++q)
+                    {
+                        const uint16_t* src = a.x + (size_t(b * cc + q) * a.nrows + row) * size_t(a.ncols) * 8;
+                        uint8_t* d = xs + i * xrow + q * kRowPlane;
+                        bulk_g2s(d, src + size_t(cl) * 8, 32, ld);
+                        bulk_g2s(d + 32, src + size_t(c0) * 8, kTile * 16, ld);
+                        bulk_g2s(d + 32 + kTile * 16, src + size_t(cr) * 8, 32, ld);
+                    }
+                }
+                for (int j = 0; j < nout; ++j)
+                    for (int q = 0; q < nq; ++q)
+                    {
+                        const uint16_t* src =
+                            a.dz + ((size_t(b * nq + q) * a.nrows + (r0 + j)) * size_t(a.ncols) + c0) * 8;
+                        bulk_g2s(dzs + j * dzrow + q * (kTile * 16), src, kTile * 16, ld);
+                    }
+                if (!mbar_wait(ld, 0, nullptr)) give_up(a.error, abort, 4);
+            }
+        }
+        else if (warp == 1)
+        {
+            if (lane == 0)
+            {
+                const uint32_t idesc = idesc_bf16(128, npad, true, true);
+                const uint32_t xa = smem_u32(xs), za = smem_u32(dzs);
+                bool ok = mbar_wait(ld, 0, abort);
+                if (ok)
+                {
+                    for (int j = 0; j < nout; ++j)
+                        for (int ks = 0; ks < kTile / 16; ++ks)
+                            for (int kx = 0; kx < 5; ++kx)
+                                for (int si = 0; si < nst; ++si)
+                                {
+                                    const uint32_t astart =
+                                        xa + (j + wg_start(cc, si)) * xrow + (ks * 16 + kx) * 16;
+                                    const uint64_t ad = smem_desc(astart, 128, kRowPlane);
+                                    const uint64_t bd = smem_desc(za + j * dzrow + ks * 256, 128, kTile * 16);
+                                    const uint32_t d = tbase + uint32_t((kx * nst + si) * npad);
+                                    mma_bf16(d, ad, bd, idesc, (j | ks) ? 1u : 0u);
+                                }
+                    mma_commit(done);
+                    if (!mbar_wait(done, 0, nullptr)) give_up(a.error, abort, 5);
+                }
+                else
+                    give_up(a.error, abort, 6);
+            }
+        }
+        else
+        {
+            const int q4 = warp & 3;
+            const int m = q4 * 32 + lane;  // accumulator row = (ky block, channel chunk, channel)
+            const int g = m >> 3, e = m & 7;
+            const int kyb = g / cc, ci = (g % cc) * 8 + e;
+            const int cin = cc * 8;
+            bool ok = mbar_wait(done, 0, abort);
+            ok = __all_sync(0xffffffffu, ok);
+            if (ok)
+            {
+                tc_fence_after();
+                for (int kx = 0; kx < 5; ++kx)
+                    for (int si = 0; si < nst; ++si)
+                    {
+                        float v[32];
+                        const uint32_t taddr = tbase + (uint32_t(q4 * 32) << 16) + uint32_t((kx * nst + si) * npad);
+                        if (npad == 32) tmem_ld32(taddr, v);
+                        else tmem_ld16(taddr, v);
+                        tmem_wait_ld();
+                        const int ky = wg_start(cc, si) + kyb;
+                        // keep each ky once: start 0 covers [0, kb), the second start only ky >= kb
+                        const bool keep = ky < 5 && (si == 0 || ky >= kb);
+                        if (keep)
+                        {
+                            float* dst = a.partial + ((size_t(blockIdx.x) * kTaps + ky * 5 + kx) * cin + ci) * npad;
+#pragma unroll
+                            for (int n = 0; n < 32; n += 4)
+                                if (n < npad)
+                                    *reinterpret_cast<float4*>(dst + n) =
+                                        make_float4(v[n], v[n + 1], v[n + 2], v[n + 3]);
+                        }
+                    }
+            }
+            else if (lane == 0)
+                give_up(a.error, abort, 7);
+        }
+
+        tc_fence_before();
+        __syncthreads();
+        if (warp == 0)
+        {
+            tc_fence_after();
+            tmem_dealloc(tbase, 512);
+        }
+    }
+
+    __global__ void wgrad_reduce_kernel(const float* __restrict__ partial, int nparts, int total, float* __restrict__ dw)
+    {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
+        {
+            float s = 0.f;
+            for (int p = 0; p < nparts; ++p) s += partial[size_t(p) * total + i];
+            dw[i] = s;
+        }
+    }
+
+    // ================================================== learned-step helpers
+    // Network input planes from the field and per-sample parameters: channel 0 =
+    // bf16(phi), 1 = 256 (phi - bf16(phi)) (the rounding remainder, so phi is
+    // carried to ~16 significant bits), 2 = zeta / 4, 3 = lambda, 4 = 10 T, 5-15 = 0.
+    __global__ void learned_input_kernel(const float* __restrict__ phi, const float* __restrict__ params, int batch,
+                                         int nrows, int ncols, uint16_t* __restrict__ x)
+    {
+        const size_t plane = size_t(nrows) * ncols;
+        const size_t n = size_t(batch) * plane;
+        for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+        {
+            const int b = int(i / plane);
+            const size_t s = i - size_t(b) * plane;
+            const float f = phi[i];
+            const __nv_bfloat16 hi = __float2bfloat16_rn(f);
+            const float lo = (f - __bfloat162float(hi)) * 256.f;
+            const float* pr = params + 3 * b;
+            uint4 c0 = make_uint4(pack_bf16x2(__bfloat162float(hi), lo), pack_bf16x2(pr[0] * 0.25f, pr[1]),
+                                  pack_bf16x2(pr[2] * 10.f, 0.f), 0u);
+            reinterpret_cast<uint4*>(x)[(size_t(b) * 2 + 0) * plane + s] = c0;
+            reinterpret_cast<uint4*>(x)[(size_t(b) * 2 + 1) * plane + s] = make_uint4(0, 0, 0, 0);
+        }
+    }
+
+    // Two standard normals per site for the macro-step noise flux, Philox keyed
+    // (seed, *step, site, component).
+    __global__ void learned_noise_kernel(float* __restrict__ xi, int nrows, int ncols, uint64_t seed,
+                                         const int64_t* __restrict__ step)
+    {
+        const int64_t st = *step;
+        const size_t plane = size_t(nrows) * ncols;
+        for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < plane; i += size_t(gridDim.x) * blockDim.x)
+        {
+            const int r = int(i / ncols), c = int(i - size_t(r) * ncols);
+            xi[i] = amb::noise_normal(seed, st, r, c, 0);
+            xi[plane + i] = amb::noise_normal(seed, st, r, c, 1);
+        }
+    }
+
+    // Face weights of the order-8 central derivative written as a difference of
+    // face sums: D8 f(j) = F(j + 1/2) - F(j - 1/2) with F(j + 1/2) = sum_e w_e f(j + e),
+    // e = -3..4, w_e = sum of c_d over d >= max(e, 1 - e), c = (4/5, -1/5, 4/105, -1/280).
+    __device__ __forceinline__ double d8_face_weight(int e)
+    {
+        const int d0 = e > 1 - e ? e : 1 - e;
+        const double c[4] = {4.0 / 5.0, -1.0 / 5.0, 4.0 / 105.0, -1.0 / 280.0};
+        double w = 0.0;
+        for (int d = d0; d <= 4; ++d) w += c[d - 1];
+        return w;
+    }
+
+    // Integer face increment through the face after site (r, c) along the axis (dr, dc).
+    __device__ __forceinline__ long long face_q(const float* __restrict__ f, const float* __restrict__ xi,
+                                                double noise_mag, double scale, int r, int c, int dr, int dc,
+                                                int nrows, int ncols)
+    {
+        double v = double(f[size_t(r) * ncols + c]);
+        if (xi)
+        {
+            double s = 0.0;
+            for (int e = -3; e <= 4; ++e)
+            {
+                int rr = r + dr * e, cc = c + dc * e;
+                rr = rr < 0 ? rr + nrows : (rr >= nrows ? rr - nrows : rr);
+                cc = cc < 0 ? cc + ncols : (cc >= ncols ? cc - ncols : cc);
+                s = __dadd_rn(s, __dmul_rn(d8_face_weight(e), double(xi[size_t(rr) * ncols + cc])));
+            }
+            v = __dadd_rn(v, __dmul_rn(noise_mag, s));
+        }
+        double q = __dmul_rn(scale, v);
+        q = q > 1e9 ? 1e9 : (q < -1e9 ? -1e9 : q);
+        return llrint(q);
+    }
+
+    // phi_q -= sum of integer face increments (each face computed identically by the two
+    // sites that share it, so the sum over all sites is unchanged: exact conservation).
+    __global__ void learned_update_kernel(const float* __restrict__ flux, const float* __restrict__ xi, int nrows,
+                                          int ncols, double scale_y, double scale_x, double noise_mag,
+                                          int32_t* __restrict__ phi_q, float* __restrict__ phi_f, long long bound,
+                                          int* __restrict__ flag)
+    {
+        const size_t plane = size_t(nrows) * ncols;
+        const float* fy = flux;
+        const float* fx = flux + plane;
+        const float* xy = xi;
+        const float* xx = xi ? xi + plane : nullptr;
+        for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < plane; i += size_t(gridDim.x) * blockDim.x)
+        {
+            const int r = int(i / ncols), c = int(i - size_t(r) * ncols);
+            const int rm = r == 0 ? nrows - 1 : r - 1, cm = c == 0 ? ncols - 1 : c - 1;
+            long long dq = face_q(fx, xx, noise_mag, scale_x, r, c, 0, 1, nrows, ncols) -
+                           face_q(fx, xx, noise_mag, scale_x, r, cm, 0, 1, nrows, ncols) +
+                           face_q(fy, xy, noise_mag, scale_y, r, c, 1, 0, nrows, ncols) -
+                           face_q(fy, xy, noise_mag, scale_y, rm, c, 1, 0, nrows, ncols);
+            long long q = (long long)phi_q[i] - dq;
+            const bool bad = !isfinite(fx[i]) || !isfinite(fy[i]) || q > bound || q < -bound;
+            if (bad)
+            {
+                atomicOr(flag, 1);
+                q = q > bound ? bound : (q < -bound ? -bound : q);
+            }
+            phi_q[i] = int32_t(q);
+            phi_f[i] = float(double(q) * (1.0 / 16777216.0));
+        }
+    }
+
+    int g_sms = 0;
+    std::once_flag g_sms_once;
+
+    int sm_count()
+    {
+        std::call_once(g_sms_once, [] {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            if (cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || g_sms < 1)
+                g_sms = 148;
+        });
+        return g_sms;
+    }
+
+    // Rows per CTA for the forward kernel: few waves of two resident CTAs per SM, each
+    // CTA paying a four-row halo.
+    int choose_fwd_rows(int batch, int nrows, int nwin)
+    {
+        const int slots = 2 * sm_count();
+        int best = 1;
+        double best_cost = 1e30;
+        for (int r = 1; r <= nrows && r <= 64; ++r)
+        {
+            const long long grid = (long long)batch * nwin * ((nrows + r - 1) / r);
+            const long long waves = (grid + slots - 1) / slots;
+            const double cost = double(waves) * (r + 4);
+            if (cost < best_cost - 1e-9)
+            {
+                best_cost = cost;
+                best = r;
+            }
+        }
+        return best;
+    }
+
+    constexpr int kWgradRows = 8;
+
+    cudaError_t set_smem_attr(const void* fn, uint32_t bytes)
+    {
+        return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+    }
+
+    bool valid_geometry(int batch, int nrows, int ncols)
+    {
+        return batch >= 1 && nrows >= 3 && ncols >= kTile && ncols % kTile == 0 &&
+               (long long)batch * nrows * ncols < (1ll << 31);
+    }
+
+    int fail_invalid(const char* what)
+    {
+        amb::set_last_error(what);
+        return AMB_ERR_INVALID;
+    }
+
+    int fail_cuda(const char* what, cudaError_t e)
+    {
+        amb::set_last_error(std::string(what) + ": " + cudaGetErrorString(e));
+        return AMB_ERR_CUDA;
+    }
+}
+
+// ============================================================= C ABI
+
+extern "C" int amb_tc_selftest(const void* a, const void* b, float* d, int n, int k, int a_mn_major, int b_mn_major,
+                               int* error, void* stream)
+{
+    if (!a || !b || !d || (n != 16 && n != 32) || k < 16 || k > 64 || k % 16 != 0)
+        return fail_invalid("amb_tc_selftest: n must be 16 or 32, k in {16, 32, 48, 64}");
+    const uint32_t smem = 98304 + 256;
+    cudaError_t e = set_smem_attr(reinterpret_cast<const void*>(tc_selftest_kernel), smem);
+    if (e == cudaSuccess)
+    {
+        tc_selftest_kernel<<<1, 128, smem, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const uint16_t*>(a), static_cast<const uint16_t*>(b), d, n, k, a_mn_major, b_mn_major, error);
+        e = cudaGetLastError();
+    }
+    return e == cudaSuccess ? AMB_OK : fail_cuda("amb_tc_selftest", e);
+}
+
+extern "C" int amb_conv5x5_forward(const void* in, int batch, int nrows, int ncols, int cin, const void* wimg,
+                                   const float* bias, int npad, int cout, int epilogue, void* out, void* pre,
+                                   const void* gate, float* out_f32, int* error, void* stream)
+{
+    if (!in || !wimg || !valid_geometry(batch, nrows, ncols) || (cin != 16 && cin != 32) ||
+        (npad != 16 && npad != 32) || epilogue < 0 || epilogue > 2)
+        return fail_invalid("amb_conv5x5_forward: need ncols % 128 == 0, nrows >= 3, cin and npad in {16, 32}");
+    if (epilogue == EPI_F32 && (!out_f32 || cout < 1 || cout > npad))
+        return fail_invalid("amb_conv5x5_forward: FP32 epilogue needs out_f32 and 1 <= cout <= npad");
+    if (epilogue != EPI_F32 && !out) return fail_invalid("amb_conv5x5_forward: bf16 epilogue needs out");
+    if (epilogue == EPI_GELU_BWD && !gate) return fail_invalid("amb_conv5x5_forward: GELU' epilogue needs gate");
+    const auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+    if (!al16(in) || !al16(wimg) || (out && !al16(out)) || (pre && !al16(pre)) || (gate && !al16(gate)))
+        return fail_invalid("amb_conv5x5_forward: bf16 buffers must be 16-byte aligned");
+
+    FwdArgs a{};
+    a.in = static_cast<const uint16_t*>(in);
+    a.wimg = static_cast<const uint16_t*>(wimg);
+    a.bias = bias;
+    a.out = static_cast<uint16_t*>(out);
+    a.pre = static_cast<uint16_t*>(pre);
+    a.gate = static_cast<const uint16_t*>(gate);
+    a.out_f32 = out_f32;
+    a.batch = batch;
+    a.nrows = nrows;
+    a.ncols = ncols;
+    a.cin_chunks = cin / 8;
+    a.npad = npad;
+    a.cout = epilogue == EPI_F32 ? cout : npad;
+    a.epilogue = epilogue;
+    const int nwin = ncols / kTile;
+    a.rows_per_cta = choose_fwd_rows(batch, nrows, nwin);
+    a.error = error;
+    const uint32_t smem = fwd_smem_bytes(a.cin_chunks, npad);
+    cudaError_t e = set_smem_attr(reinterpret_cast<const void*>(conv_fwd_kernel), fwd_smem_bytes(4, 32));
+    if (e == cudaSuccess)
+    {
+        const long long grid = (long long)batch * nwin * ((nrows + a.rows_per_cta - 1) / a.rows_per_cta);
+        conv_fwd_kernel<<<unsigned(grid), kThreads, smem, static_cast<cudaStream_t>(stream)>>>(a);
+        e = cudaGetLastError();
+    }
+    return e == cudaSuccess ? AMB_OK : fail_cuda("amb_conv5x5_forward", e);
+}
+
+static long long wgrad_grid(int batch, int nrows, int ncols)
+{
+    return (long long)batch * (ncols / kTile) * ((nrows + kWgradRows - 1) / kWgradRows);
+}
+
+extern "C" size_t amb_conv5x5_wgrad_scratch_bytes(int batch, int nrows, int ncols, int cin, int npad)
+{
+    if (!valid_geometry(batch, nrows, ncols)) return 0;
+    return size_t(wgrad_grid(batch, nrows, ncols)) * kTaps * cin * npad * sizeof(float);
+}
+
+extern "C" int amb_conv5x5_wgrad(const void* x, const void* dz, int batch, int nrows, int ncols, int cin, int npad,
+                                 float* dw, float* scratch, size_t scratch_bytes, int* error, void* stream)
+{
+    if (!x || !dz || !dw || !scratch || !valid_geometry(batch, nrows, ncols) || (cin != 16 && cin != 32) ||
+        (npad != 16 && npad != 32))
+        return fail_invalid("amb_conv5x5_wgrad: need ncols % 128 == 0, nrows >= 3, cin and npad in {16, 32}");
+    if (scratch_bytes < amb_conv5x5_wgrad_scratch_bytes(batch, nrows, ncols, cin, npad))
+        return fail_invalid("amb_conv5x5_wgrad: scratch too small (see amb_conv5x5_wgrad_scratch_bytes)");
+    WgradArgs a{};
+    a.x = static_cast<const uint16_t*>(x);
+    a.dz = static_cast<const uint16_t*>(dz);
+    a.partial = scratch;
+    a.batch = batch;
+    a.nrows = nrows;
+    a.ncols = ncols;
+    a.cin_chunks = cin / 8;
+    a.npad = npad;
+    a.rows_per_cta = kWgradRows;
+    a.error = error;
+    const uint32_t smem = wg_smem_bytes(a.cin_chunks, npad, kWgradRows);
+    cudaError_t e = set_smem_attr(reinterpret_cast<const void*>(conv_wgrad_kernel),
+                                  std::max(wg_smem_bytes(4, 32, kWgradRows), wg_smem_bytes(2, 32, kWgradRows)));
+    auto s = static_cast<cudaStream_t>(stream);
+    const long long grid = wgrad_grid(batch, nrows, ncols);
+    if (e == cudaSuccess)
+    {
+        conv_wgrad_kernel<<<unsigned(grid), kThreads, smem, s>>>(a);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+    {
+        const int total = kTaps * cin * npad;
+        wgrad_reduce_kernel<<<(total + 255) / 256, 256, 0, s>>>(scratch, int(grid), total, dw);
+        e = cudaGetLastError();
+    }
+    return e == cudaSuccess ? AMB_OK : fail_cuda("amb_conv5x5_wgrad", e);
+}
+
+extern "C" int amb_learned_input(const float* phi, const float* params, int batch, int nrows, int ncols, void* x,
+                                 void* stream)
+{
+    if (!phi || !params || !x || !valid_geometry(batch, nrows, ncols))
+        return fail_invalid("amb_learned_input: bad arguments");
+    const size_t n = size_t(batch) * nrows * ncols;
+    const int grid = int(std::min<size_t>((n + 255) / 256, size_t(sm_count()) * 16));
+    learned_input_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(phi, params, batch, nrows, ncols,
+                                                                            static_cast<uint16_t*>(x));
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_input", e);
+}
+
+extern "C" int amb_learned_update(const float* flux, int nrows, int ncols, double dt_macro, double dx, double dy,
+                                  double temperature, uint64_t seed, const int64_t* step, float* xi_scratch,
+                                  int32_t* phi_q, float* phi_f, double bound, int* flag, void* stream)
+{
+    if (!flux || !phi_q || !phi_f || !flag || nrows < 1 || ncols < 1 || !(dt_macro > 0) || !(dx > 0) ||
+        !(dy > 0) || temperature < 0 || !(bound > 0) || (temperature > 0 && (!step || !xi_scratch)))
+        return fail_invalid("amb_learned_update: bad arguments");
+    auto s = static_cast<cudaStream_t>(stream);
+    const size_t n = size_t(nrows) * ncols;
+    const int grid = int(std::min<size_t>((n + 255) / 256, size_t(sm_count()) * 16));
+    const bool noisy = temperature > 0;
+    if (noisy) learned_noise_kernel<<<grid, 256, 0, s>>>(xi_scratch, nrows, ncols, seed, step);
+    const double fix = 16777216.0;
+    const double noise_mag = noisy ? std::sqrt(2.0 * temperature) * std::sqrt(1.0 / (dt_macro * dx * dy)) : 0.0;
+    const double qb = std::min(bound * fix, 2.0e9);
+    learned_update_kernel<<<grid, 256, 0, s>>>(flux, noisy ? xi_scratch : nullptr, nrows, ncols, dt_macro / dy * fix,
+                                               dt_macro / dx * fix, noise_mag, phi_q, phi_f, (long long)qb, flag);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_update", e);
+}

@@ -203,6 +203,11 @@ void amb_ensemble_destroy(amb_ensemble* h);
 int amb_ensemble_run(amb_ensemble* h, int nsteps);
 int amb_ensemble_get_field(amb_ensemble* h, int replica, double* host_out);
 int amb_ensemble_info(const amb_ensemble* h, int64_t* timestep, int* ntasks, int* seg_rows);
+/* Device-to-device copy of every replica's current field into dst / from src (FP32, packed
+ * back to back in replica order, replica r at offset sum_{q<r} nrows_q*ncols_q). Scatter also
+ * zeroes the compensation residuals. Synchronous. */
+int amb_ensemble_gather(amb_ensemble* h, float* dst);
+int amb_ensemble_scatter(amb_ensemble* h, const float* src);
 
 /* ================================================================ analysis */
 
@@ -222,6 +227,65 @@ int amb_label_components_f64(const double* field, int nrows, int ncols, double t
                              void* stream);
 int amb_label_components_f32(const float* field, int nrows, int ncols, double threshold, int* labels, int* ncomp,
                              void* stream);
+
+
+/* ========================================================== learned stepper */
+/* No reference counterpart. Building blocks of the learned coarse stepper: a
+ * periodic CNN of 5x5 circular convolutions that predicts a face flux over many
+ * Euler steps. All buffers are DEVICE pointers; calls are stream-ordered.
+ *
+ * Activations are bf16 "chunk planes": [batch][C/8][nrows][ncols][8] (16-byte
+ * aligned). Requirements: ncols % 128 == 0, nrows >= 3, C in {16, 32}.
+ * Convolution weights are passed as a bf16 B-operand image
+ * [25 taps (ky*5+kx)][Cin/8][npad][8]: element (tap, ci, co) at
+ * ((tap*Cin/8 + ci/8)*npad + co)*8 + ci%8, co < npad zero-padded.
+ * *error (device int, may be NULL) receives a non-zero code if a kernel gave up
+ * waiting on its own pipeline (the outputs are then incomplete). */
+
+/* Tensor-core self-test: d (128 x n, row-major FP32) = a (128 x k) * b (n x k)^T,
+ * a and b row-major bf16, staged K-major (flag 0) or MN-major (flag 1).
+ * n in {16, 32}, k in {16, 32, 48, 64}. One CTA. */
+int amb_tc_selftest(const void* a, const void* b, float* d, int n, int k, int a_mn_major, int b_mn_major, int* error,
+                    void* stream);
+
+/* Epilogues of amb_conv5x5_forward */
+#define AMB_EPI_GELU 0     /* out = bf16(gelu(acc + bias)); pre (optional) = bf16(acc + bias) */
+#define AMB_EPI_F32 1      /* out_f32[batch][cout][nrows][ncols] = acc + bias (first cout channels) */
+#define AMB_EPI_GELU_BWD 2 /* out = bf16(acc * gelu'(gate)), gate = pre-activation, same layout as out */
+
+/* Circular 5x5 convolution, BF16 tensor cores, FP32 accumulation:
+ * acc[b][co][r][c] = sum_{ci,ky,kx} w[co][ci][ky][kx] in[b][ci][(r+ky-2) mod nrows][(c+kx-2) mod ncols].
+ * in: [batch][cin/8][nrows][ncols][8]; out/pre/gate: [batch][npad/8][nrows][ncols][8]. The data
+ * gradient of the same convolution is this call with the kernel flipped in (ky, kx) and the
+ * channel roles swapped. */
+int amb_conv5x5_forward(const void* in, int batch, int nrows, int ncols, int cin, const void* wimg, const float* bias,
+                        int npad, int cout, int epilogue, void* out, void* pre, const void* gate, float* out_f32,
+                        int* error, void* stream);
+
+/* Weight gradient: dw[tap][ci][co] (FP32, 25*cin*npad) = sum over batch and sites of
+ * x[b][ci][(r+ky-2) mod nrows][(c+kx-2) mod ncols] * dz[b][co][r][c]. x: [batch][cin/8][...][8],
+ * dz: [batch][npad/8][...][8]. Deterministic (fixed reduction order); scratch must hold
+ * amb_conv5x5_wgrad_scratch_bytes(...) bytes. */
+size_t amb_conv5x5_wgrad_scratch_bytes(int batch, int nrows, int ncols, int cin, int npad);
+int amb_conv5x5_wgrad(const void* x, const void* dz, int batch, int nrows, int ncols, int cin, int npad, float* dw,
+                      float* scratch, size_t scratch_bytes, int* error, void* stream);
+
+/* Network input planes (16 channels, 2 chunks): bf16(phi), 256*(phi - bf16(phi)), zeta/4,
+ * lambda, 10*T, zeros. phi: [batch][nrows][ncols] FP32; params: [batch][3] = (zeta, lambda, T). */
+int amb_learned_input(const float* phi, const float* params, int batch, int nrows, int ncols, void* x, void* stream);
+
+/* One macro step of the learned stepper on a fixed-point field phi_q (int32, phi * 2^24):
+ * phi -= dt_macro * div F, F = flux + noise flux, with div the face difference
+ * (F_x(r,c) - F_x(r,c-1))/dx + (F_y(r,c) - F_y(r-1,c))/dy. flux: [2][nrows][ncols] FP32
+ * (component 0 = y face after (r,c), 1 = x face). For temperature > 0 the noise flux is the
+ * order-8 central derivative of sqrt(2T/(dt_macro dx dy)) xi written as face sums, xi
+ * Philox normals keyed (seed, *step, site) (xi_scratch: 2*nrows*ncols floats). Every face
+ * increment is rounded to an integer once and applied with opposite signs to its two sites,
+ * so sum(phi_q) is conserved exactly. phi_f receives phi_q * 2^-24. *flag |= 1 if the flux is
+ * non-finite or |phi| exceeds bound (then clamped). */
+int amb_learned_update(const float* flux, int nrows, int ncols, double dt_macro, double dx, double dy,
+                       double temperature, uint64_t seed, const int64_t* step, float* xi_scratch, int32_t* phi_q,
+                       float* phi_f, double bound, int* flag, void* stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,288 @@
+"""Learned stepper on the GPU: the tcgen05 kernels against the CPU FP64 oracle
+(oracle/learned.py), the exact fixed-point update, and what training gains.
+
+Tolerances: FP32 accumulation of <= 800 bf16 products gives ~1e-6 relative error
+on FP32 outputs; bf16 outputs carry one bf16 rounding (relative 2^-8); network
+gradients carry the bf16 rounding of every stored activation and gradient."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle.learned as OL
+
+pytestmark = pytest.mark.gpu
+
+
+def mods():
+    import torch
+    from activemodelbplus import learned as L
+    from activemodelbplus.integrator import _native as N
+    return torch, L, N
+
+
+def bf16(a):
+    torch = mods()[0]
+    return torch.from_numpy(np.asarray(a, dtype=np.float32)).to(torch.bfloat16).cuda()
+
+
+# ------------------------------------------------------------ self-test
+
+@pytest.mark.parametrize("a_mn,b_mn", [(0, 0), (1, 1), (0, 1), (1, 0)])
+@pytest.mark.parametrize("n,k", [(32, 16), (16, 64), (32, 64)])
+def test_tensor_core_selftest(a_mn, b_mn, n, k):
+    """One 128 x n x k GEMM through tcgen05 with the operands in the K-major and the
+    MN-major core-matrix layouts: D = A B^T to FP32 accumulation accuracy."""
+    torch, L, N = mods()
+    rng = np.random.default_rng(n * k + a_mn * 2 + b_mn)
+    A = OL.bf16_round(rng.standard_normal((128, k)))
+    B = OL.bf16_round(rng.standard_normal((n, k)))
+    d = torch.zeros(128, n, dtype=torch.float32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    a_dev, b_dev = bf16(A), bf16(B)  # keep both alive until the kernel has run
+    rc = N.lib().amb_tc_selftest(a_dev.data_ptr(), b_dev.data_ptr(), d.data_ptr(), n, k, a_mn, b_mn,
+                                 err.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, N.last_error()
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    ref = A @ B.T
+    assert np.abs(d.cpu().numpy() - ref).max() < 1e-4
+
+
+# ------------------------------------------------------------ convolutions
+
+def run_conv(x, w, b, *, cin, npad, cout, epilogue, gate=None, with_pre=False):
+    torch, L, N = mods()
+    xc = L.to_chunks(torch.from_numpy(x).float().cuda(), cin)
+    img = L.weight_image(torch.from_numpy(w).float().cuda(), cin, npad)
+    bias = None
+    if b is not None:
+        bias = torch.zeros(npad, dtype=torch.float32, device="cuda")
+        bias[: len(b)] = torch.from_numpy(np.asarray(b, dtype=np.float32)).cuda()
+    B, _, H, W = x.shape
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    if epilogue == N.AMB_EPI_F32:
+        out = torch.empty(B, cout, H, W, dtype=torch.float32, device="cuda")
+        L.conv_forward(xc, img, bias, cin=cin, npad=npad, cout=cout, epilogue=epilogue, out_f32=out, error=err)
+        torch.cuda.synchronize()
+        assert int(err.item()) == 0
+        return out.cpu().numpy().astype(np.float64), None
+    out = torch.empty(B, npad // 8, H, W, 8, dtype=torch.bfloat16, device="cuda")
+    pre = torch.empty_like(out) if with_pre else None
+    g = None if gate is None else L.to_chunks(torch.from_numpy(gate).float().cuda(), npad)
+    L.conv_forward(xc, img, bias, cin=cin, npad=npad, epilogue=epilogue, out=out, pre=pre, gate=g, error=err)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    o = L.from_chunks(out, npad).cpu().numpy().astype(np.float64)
+    p = None if pre is None else L.from_chunks(pre, npad).cpu().numpy().astype(np.float64)
+    return o, p
+
+
+SHAPES = [(2, 16, 128), (1, 20, 256), (3, 7, 128), (1, 3, 384), (1, 130, 128)]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("cin_used,cin,cout,npad", [(5, 16, 32, 32), (32, 32, 32, 32), (32, 32, 2, 16),
+                                                    (16, 16, 16, 16)])
+def test_conv_forward_f32(shape, cin_used, cin, cout, npad):
+    B, H, W = shape
+    rng = np.random.default_rng(H * W + cin + npad)
+    x = OL.bf16_round(rng.standard_normal((B, cin_used, H, W)))
+    w = OL.bf16_round(rng.standard_normal((cout, cin_used, 5, 5)) * 0.1)
+    b = rng.standard_normal(cout).astype(np.float32)
+    got, _ = run_conv(x, w, b, cin=cin, npad=npad, cout=cout, epilogue=1)
+    ref = OL.conv5x5(x, w, b.astype(np.float64))
+    assert np.abs(got - ref).max() < 2e-5 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("shape", SHAPES[:3])
+def test_conv_forward_gelu(shape):
+    B, H, W = shape
+    rng = np.random.default_rng(5)
+    x = OL.bf16_round(rng.standard_normal((B, 32, H, W)))
+    w = OL.bf16_round(rng.standard_normal((32, 32, 5, 5)) * 0.05)
+    b = rng.standard_normal(32).astype(np.float32) * 0.1
+    out, pre = run_conv(x, w, b, cin=32, npad=32, cout=32, epilogue=0, with_pre=True)
+    z = OL.conv5x5(x, w, b.astype(np.float64))
+    assert np.abs(pre - z).max() <= 2.0 ** -8 * np.abs(z).max() + 1e-6
+    a = OL.gelu(z)
+    assert np.abs(out - a).max() <= 2.0 ** -8 * np.abs(a).max() + 1e-5
+
+
+@pytest.mark.parametrize("cin_fwd,npad_fwd,cout_used", [(32, 32, 32), (32, 16, 2)])
+def test_conv_data_gradient(cin_fwd, npad_fwd, cout_used):
+    """dgrad through the GELU of the layer below: conv of dz with the flipped, channel-swapped
+    image, times gelu'(gate), against FP64 autograd."""
+    torch, L, N = mods()
+    rng = np.random.default_rng(cout_used)
+    B, H, W = 2, 12, 128
+    w = rng.standard_normal((cout_used, 32, 5, 5)) * 0.05
+    dz = OL.bf16_round(rng.standard_normal((B, cout_used, H, W)))
+    gate = OL.bf16_round(rng.standard_normal((B, 32, H, W)))
+    wt = torch.from_numpy(w).float().cuda()
+    img = L.dgrad_image(wt, cin_fwd, npad_fwd)
+    dzc = L.to_chunks(torch.from_numpy(dz).float().cuda(), npad_fwd)
+    gc = L.to_chunks(torch.from_numpy(gate).float().cuda(), cin_fwd)
+    out = torch.empty(B, cin_fwd // 8, H, W, 8, dtype=torch.bfloat16, device="cuda")
+    L.conv_forward(dzc, img, None, cin=npad_fwd, npad=cin_fwd, epilogue=N.AMB_EPI_GELU_BWD, out=out, gate=gc)
+    got = L.from_chunks(out, 32).cpu().numpy().astype(np.float64)
+    dx, _ = OL.conv5x5_grads(np.zeros((B, 32, H, W)), OL.bf16_round(w), dz)
+    ref = dx * OL.gelu_grad(gate)
+    assert np.abs(got - ref).max() <= 2.0 ** -7 * np.abs(ref).max() + 1e-6
+
+
+@pytest.mark.parametrize("shape", [(2, 16, 128), (1, 13, 256), (1, 9, 384)])
+@pytest.mark.parametrize("cin_used,cin,cout,npad", [(32, 32, 32, 32), (5, 16, 32, 32), (32, 32, 2, 16)])
+def test_conv_weight_gradient(shape, cin_used, cin, cout, npad):
+    torch, L, N = mods()
+    B, H, W = shape
+    rng = np.random.default_rng(H + cin + npad)
+    x = OL.bf16_round(rng.standard_normal((B, cin_used, H, W)))
+    dz = OL.bf16_round(rng.standard_normal((B, cout, H, W)))
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    dw = L.conv_wgrad(L.to_chunks(torch.from_numpy(x).float().cuda(), cin),
+                      L.to_chunks(torch.from_numpy(dz).float().cuda(), npad), cin=cin, npad=npad, error=err)
+    got = L.wgrad_to_weights(dw, cout, cin_used).cpu().numpy().astype(np.float64)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    _, ref = OL.conv5x5_grads(x, np.zeros((cout, cin_used, 5, 5)), dz)
+    assert np.abs(got - ref).max() < 2e-5 * max(1.0, np.abs(ref).max())
+
+
+def test_wgrad_is_deterministic():
+    torch, L, N = mods()
+    rng = np.random.default_rng(3)
+    x = L.to_chunks(torch.from_numpy(rng.standard_normal((4, 32, 32, 128))).float().cuda(), 32)
+    dz = L.to_chunks(torch.from_numpy(rng.standard_normal((4, 32, 32, 128))).float().cuda(), 32)
+    a = L.conv_wgrad(x, dz, cin=32, npad=32)
+    b = L.conv_wgrad(x, dz, cin=32, npad=32)
+    assert torch.equal(a, b)
+
+
+# ------------------------------------------------------------ network
+
+def test_network_forward_and_gradients_match_oracle():
+    """Whole flux network, forward + backward on the device kernels vs FP64 autograd with
+    the same bf16 rounding points: flux to 5e-3 relative, gradients to 3e-2 relative (L2).
+    (FP32 accumulation differs from FP64 by ~1e-5 relative per layer; where that moves a value
+    across a bf16 rounding boundary the stored activation differs by 2^-8 relative, and such
+    flips compound over six layers to ~1e-3.)"""
+    torch, L, N = mods()
+    net = L.FluxNet(seed=1)
+    for w in net.weights:
+        w.mul_(1.5)
+    net.refresh()
+    rng = np.random.default_rng(4)
+    B, H, W = 2, 16, 128
+    phi = (-0.3 + 0.5 * rng.standard_normal((B, H, W))).astype(np.float32)
+    params = np.array([[-2.0, 0.5, 0.05], [1.0, -0.7, 0.0]], dtype=np.float32)
+    x = L.network_input(torch.from_numpy(phi).cuda(), torch.from_numpy(params).cuda())
+    xin = OL.network_input(phi, params)
+    assert np.array_equal(L.from_chunks(x, 5).cpu().numpy().astype(np.float64), OL.bf16_round(xin))
+    flux = net.forward(x, train=True)
+    dflux = rng.standard_normal((B, 2, H, W)).astype(np.float32)
+    gw, gb = net.backward(torch.from_numpy(dflux).cuda())
+    net.check_error()
+    ws = [w.cpu().numpy().astype(np.float64) for w in net.weights]
+    bs = [b.cpu().numpy().astype(np.float64) for b in net.biases]
+    rflux, rgw, rgb = OL.fluxnet(xin, ws, bs, dflux.astype(np.float64))
+    f = flux.cpu().numpy()
+    assert np.linalg.norm(f - rflux) <= 5e-3 * np.linalg.norm(rflux)
+    for l in range(6):
+        g = gw[l].cpu().numpy()
+        assert np.linalg.norm(g - rgw[l]) <= 3e-2 * np.linalg.norm(rgw[l]), l
+        gbl = gb[l].cpu().numpy()[: len(rgb[l])]
+        assert np.linalg.norm(gbl - rgb[l]) <= 3e-2 * np.linalg.norm(rgb[l]), l
+
+
+# ------------------------------------------------------------ fixed-point update
+
+@pytest.mark.parametrize("T", [0.0, 0.05])
+def test_update_is_exact_and_conservative(T):
+    torch, L, N = mods()
+    rng = np.random.default_rng(6)
+    H, W = 48, 128
+    phi_q = np.rint(rng.uniform(-0.8, 0.8, (H, W)) * OL.FIX).astype(np.int32)
+    flux = (0.3 * rng.standard_normal((2, H, W))).astype(np.float32)
+    q = torch.from_numpy(phi_q).cuda()
+    f = torch.empty(H, W, dtype=torch.float32, device="cuda")
+    xi = torch.empty(2, H, W, dtype=torch.float32, device="cuda")
+    step = torch.tensor([7], dtype=torch.int64, device="cuda")
+    flag = torch.zeros(1, dtype=torch.int32, device="cuda")
+    dtk = 0.05
+    flux_dev = torch.from_numpy(flux).cuda()
+    rc = N.lib().amb_learned_update(flux_dev.data_ptr(), H, W, dtk, 1.0, 1.0, T, 99,
+                                    step.data_ptr(), xi.data_ptr(), q.data_ptr(), f.data_ptr(), 3.0,
+                                    flag.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, N.last_error()
+    got = q.cpu().numpy().astype(np.int64)
+    if T > 0:
+        mag = math.sqrt(2 * T) * math.sqrt(1 / (dtk * 1.0 * 1.0))
+        ref = OL.face_update(phi_q, flux, dtk, xi=xi.cpu().numpy(), noise_mag=mag)
+        import oracle
+        xy, xx = oracle.normals(H, W, 99, 7)  # the same Philox-keyed normals, evaluated in double
+        assert np.abs(xi.cpu().numpy() - np.stack([xy, xx])).max() < 5e-5
+    else:
+        ref = OL.face_update(phi_q, flux, dtk)
+    assert np.array_equal(got, ref)
+    assert got.sum() == phi_q.astype(np.int64).sum()
+    assert np.array_equal(f.cpu().numpy(), (got / OL.FIX).astype(np.float32))
+    assert int(flag.item()) == 0
+
+
+# ------------------------------------------------------------ stepper and training gain
+
+def test_stepper_conserves_and_falls_back():
+    """An untrained network fails the residual check, so every span is redone by the plain
+    integrator; the fixed-point mass is unchanged by learned macro steps."""
+    torch, L, N = mods()
+    from activemodelbplus.integrator import Model, Stencil
+    rng = np.random.default_rng(7)
+    field = -0.4 + 0.01 * rng.standard_normal((64, 128))
+    net = L.FluxNet(seed=3)
+    st = L.LearnedStepper(net, field, Stencil(1e-3, 1, 1), Model(-0.25, 0, 0.25, 1, -1, -4, 0.0), K=50,
+                          check_every=4, tol=0.05)
+    m0 = st.mass_q()
+    st.advance(8)
+    assert st.fallback_spans == 2 and st.learned_steps == 0
+    assert st.macro_steps == 8 and np.isfinite(st.field).all()
+    st.tol = 1e9  # accept everything: pure learned steps, exact conservation
+    m1 = st.mass_q()
+    st.advance(8)
+    assert st.learned_steps == 8
+    assert st.mass_q() == m1
+    assert abs(m1 - m0) < 64 * 128  # plain FP32 spans conserve to rounding
+
+
+def test_training_gains_over_untrained_and_naive_coarse_step():
+    """A short training run on plain-integrator pairs: the trained flux predicts the
+    deterministic 50-step increment far better than the untrained network and than one
+    explicit Euler step of size 50 dt (the method without the network)."""
+    torch, L, N = mods()
+    from activemodelbplus.integrator import Integrator, Model, Stencil
+    K, dt = 50, 1e-3
+    phi, delta, params, models = L.generate_pairs(48, 128, K, [2000, 6000, 12000], seed=11)
+    tr = (phi[:, :40], delta[:, :40], params[:40])
+    te = (phi[:, 40:], delta[:, 40:], params[40:])
+    net = L.FluxNet(seed=0)
+    before = L.evaluate(net, *te, K=K, dt=dt)
+    L.train(net, *tr, K=K, dt=dt, iters=400, batch=8, lr=2e-3)
+    after = L.evaluate(net, *te, K=K, dt=dt)
+    # naive: one Euler step with dt' = K dt from the same states (deterministic)
+    num = den = 0.0
+    for s in range(phi.shape[0]):
+        for i in range(40, 48):
+            m = models[i]
+            quiet = Model(m.a, m.b, m.c, m.kappa, m.lamb, m.zeta, 0.0)
+            sim = Integrator(phi[s, i].cpu().numpy(), Stencil(K * dt, 1, 1), quiet, precision="f64")
+            try:
+                sim.run(1)
+                pred = sim.field - phi[s, i].cpu().numpy()
+            except Exception:
+                pred = np.full(phi.shape[2:], np.inf)
+            d = delta[s, i].cpu().numpy().astype(np.float64)
+            num += float(np.square(pred - d).sum())
+            den += float(np.square(d).sum())
+    naive = num / den
+    assert after < 0.5 * before, (before, after)
+    assert after < naive, (after, naive)

@@ -1,0 +1,137 @@
+"""Learned stepper, host side, no GPU: the operand layouts the tensor-core kernels
+read (chunk planes, B-operand weight images, the flipped data-gradient image,
+the weight-gradient output order) checked by emulating the kernels' index
+arithmetic in numpy against the FP64 oracle; and the fixed-point face update's
+exact conservation."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import oracle.learned as OL
+from activemodelbplus import learned as L
+
+
+def emulate_conv(xc, img, npad):
+    """What amb_conv5x5_forward computes, from the same buffers: for output site (r, c),
+    tap (ky, kx) reads staged site m + kx of input row r + ky - 2 (A operand, K-major over
+    the channel chunks) against image[tap][chunk][co][e] (B operand)."""
+    xc = xc.float().numpy().astype(np.float64)      # [B, q, H, W, 8]
+    im = img.float().numpy().astype(np.float64)     # [25, q, npad, 8]
+    B, q, H, W, _ = xc.shape
+    out = np.zeros((B, npad, H, W))
+    for ky in range(5):
+        for kx in range(5):
+            xs = np.roll(xc, shift=(-(ky - 2), -(kx - 2)), axis=(2, 3))  # xs[r, c] = x[r+ky-2, c+kx-2]
+            out += np.einsum("bqhwe,qne->bnhw", xs, im[ky * 5 + kx])
+    return out
+
+
+def emulate_wgrad(xc, dzc):
+    """What amb_conv5x5_wgrad computes: dw[tap][ci][co] = sum_sites x[ci][site + tap] dz[co][site]."""
+    x = L.from_chunks(xc, xc.shape[1] * 8).numpy().astype(np.float64)
+    dz = L.from_chunks(dzc, dzc.shape[1] * 8).numpy().astype(np.float64)
+    dw = np.zeros((25, x.shape[1], dz.shape[1]))
+    for ky in range(5):
+        for kx in range(5):
+            xs = np.roll(x, shift=(-(ky - 2), -(kx - 2)), axis=(2, 3))
+            dw[ky * 5 + kx] = np.einsum("bihw,bohw->io", xs, dz)
+    return torch.from_numpy(dw)
+
+
+def _rand(shape, seed):
+    return torch.from_numpy(np.random.default_rng(seed).standard_normal(shape))
+
+
+def test_bf16_round_matches_torch():
+    v = np.random.default_rng(0).standard_normal(1000) * 10.0 ** np.random.default_rng(1).integers(-5, 5, 1000)
+    assert np.array_equal(OL.bf16_round(v), torch.from_numpy(v).float().to(torch.bfloat16).double().numpy())
+
+
+def test_chunk_layout_round_trip():
+    x = _rand((2, 5, 6, 8), 1).float()
+    xc = L.to_chunks(x, 16)
+    assert tuple(xc.shape) == (2, 2, 6, 8, 8) and xc.dtype == torch.bfloat16
+    back = L.from_chunks(xc, 5)
+    assert torch.equal(back, x.to(torch.bfloat16).float())
+    assert torch.all(L.from_chunks(xc, 16)[:, 5:] == 0)
+
+
+@pytest.mark.parametrize("cin_used,cin,cout,npad", [(5, 16, 32, 32), (32, 32, 32, 32), (32, 32, 2, 16), (12, 16, 7, 16)])
+def test_forward_image_layout(cin_used, cin, cout, npad):
+    x = _rand((2, cin_used, 7, 9), 2).float()
+    w = _rand((cout, cin_used, 5, 5), 3).float()
+    got = emulate_conv(L.to_chunks(x, cin), L.weight_image(w, cin, npad), npad)
+    ref = OL.conv5x5(OL.bf16_round(x.numpy()), OL.bf16_round(w.numpy()))
+    assert np.abs(got[:, :cout] - ref).max() < 1e-9 * max(1.0, np.abs(ref).max())
+    assert np.all(got[:, cout:] == 0)
+
+
+@pytest.mark.parametrize("cin,npad,cout_used", [(32, 32, 32), (32, 16, 2), (16, 32, 32)])
+def test_dgrad_image_is_the_data_gradient(cin, npad, cout_used):
+    """Data gradient = forward convolution of the output gradient with the flipped,
+    channel-swapped image."""
+    cin_used = 5 if cin == 16 else cin
+    w = _rand((cout_used, cin_used, 5, 5), 4).float()
+    x = _rand((2, cin_used, 6, 7), 5)
+    dz = _rand((2, cout_used, 6, 7), 6).float()
+    wr, dzr = OL.bf16_round(w.numpy()), OL.bf16_round(dz.numpy())
+    dx_ref, _ = OL.conv5x5_grads(x.numpy(), wr, dzr)
+    got = emulate_conv(L.to_chunks(dz, npad), L.dgrad_image(w, cin, npad), cin)
+    assert np.abs(got[:, :cin_used] - dx_ref).max() < 1e-9 * max(1.0, np.abs(dx_ref).max())
+
+
+@pytest.mark.parametrize("cin,cin_used,npad,cout", [(32, 32, 32, 32), (16, 5, 32, 32), (32, 32, 16, 2)])
+def test_wgrad_output_order(cin, cin_used, npad, cout):
+    x = _rand((2, cin_used, 6, 7), 7).float()
+    dz = _rand((2, cout, 6, 7), 8).float()
+    dw = emulate_wgrad(L.to_chunks(x, cin), L.to_chunks(dz, npad))
+    got = L.wgrad_to_weights(dw, cout, cin_used).numpy()
+    _, dw_ref = OL.conv5x5_grads(OL.bf16_round(x.numpy()), np.zeros((cout, cin_used, 5, 5)),
+                                 OL.bf16_round(dz.numpy()))
+    assert np.abs(got - dw_ref).max() < 1e-9 * max(1.0, np.abs(dw_ref).max())
+
+
+def test_d8_face_sums_reproduce_the_central_difference():
+    f = np.random.default_rng(9).standard_normal(64)
+    w = OL.d8_face_weights()
+    F = sum(w[i] * np.roll(f, -e) for i, e in enumerate(range(-3, 5)))  # F(j + 1/2)
+    d8 = sum(c * (np.roll(f, -d) - np.roll(f, d)) for d, c in zip(range(1, 5), OL.D8))
+    assert np.abs((F - np.roll(F, 1)) - d8).max() < 1e-14
+
+
+def test_face_update_conserves_exactly():
+    rng = np.random.default_rng(10)
+    phi_q = np.rint(rng.uniform(-1, 1, (24, 40)) * OL.FIX).astype(np.int64)
+    flux = rng.standard_normal((2, 24, 40)).astype(np.float32)
+    xi = rng.standard_normal((2, 24, 40)).astype(np.float32)
+    for kw in ({}, {"xi": xi, "noise_mag": 3.0}):
+        new = OL.face_update(phi_q, flux, 0.05, **kw)
+        assert new.sum() == phi_q.sum()
+        assert not np.array_equal(new, phi_q)
+
+
+def test_network_oracle_gradients_match_finite_differences():
+    """The FP64 network oracle's backward (no bf16 rounding) against central differences."""
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal((1, 5, 6, 6))
+    ws = [rng.standard_normal((4, 5, 5, 5)) * 0.1, rng.standard_normal((2, 4, 5, 5)) * 0.1]
+    bs = [rng.standard_normal(4) * 0.1, rng.standard_normal(2) * 0.1]
+    dflux = rng.standard_normal((1, 2, 6, 6))
+    _, gw, gb = OL.fluxnet(x, ws, bs, dflux, bf16_activations=False)
+    eps = 1e-6
+    for l, (i, j, ky, kx) in ((0, (1, 2, 3, 4)), (1, (0, 3, 2, 2))):
+        wp = [w.copy() for w in ws]
+        wm = [w.copy() for w in ws]
+        wp[l][i, j, ky, kx] += eps
+        wm[l][i, j, ky, kx] -= eps
+        fp = (OL.fluxnet(x, wp, bs, bf16_activations=False) * dflux).sum()
+        fm = (OL.fluxnet(x, wm, bs, bf16_activations=False) * dflux).sum()
+        assert abs((fp - fm) / (2 * eps) - gw[l][i, j, ky, kx]) < 1e-6
+    bp = [b.copy() for b in bs]
+    bp[0][1] += eps
+    bm = [b.copy() for b in bs]
+    bm[0][1] -= eps
+    fd = ((OL.fluxnet(x, ws, bp, bf16_activations=False) - OL.fluxnet(x, ws, bm, bf16_activations=False))
+          * dflux).sum() / (2 * eps)
+    assert abs(fd - gb[0][1]) < 1e-6
