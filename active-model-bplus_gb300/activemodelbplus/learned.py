@@ -7,7 +7,7 @@ that advances the field by K explicit-Euler steps at once:
 
 Because the update is a difference of face fluxes, applied in int32 fixed point
 (phi * 2^24) with each face rounded once, the sum of the field is conserved
-exactly. The network is 6 circular 5x5 convolutions, 32 channels, GELU, BF16
+exactly. The network is 6 circular 5x5 convolutions, 32 channels, GELU (tanh form), BF16
 weights and activations with FP32 accumulation; its forward and both backward
 passes run on this package's own tcgen05 implicit-GEMM kernels
 (``amb_conv5x5_forward`` / ``amb_conv5x5_wgrad``). Training targets are the
@@ -69,14 +69,15 @@ def from_chunks(xc, c: int):
 
 
 def weight_image(w, cin_pad: int, npad: int):
-    """Convolution weights [cout, cin, 5, 5] -> the kernels' bf16 B-operand image
-    [25][cin_pad/8][npad][8] (zero padded)."""
+    """Convolution weights [cout, cin, 5, 5] (ky, kx) -> the kernels' bf16 B-operand image
+    [5 kx][cin_pad/8][5 (4 - ky)][npad][8] (zero padded): for each x tap and channel chunk,
+    the five y taps stacked along N in reverse order."""
     torch = _torch()
     cout, cin = w.shape[:2]
     wp = torch.zeros(npad, cin_pad, 5, 5, dtype=torch.float32, device=w.device)
     wp[:cout, :cin] = w
-    img = wp.reshape(npad, cin_pad // 8, 8, 5, 5).permute(3, 4, 1, 0, 2).contiguous()
-    return img.reshape(25, cin_pad // 8, npad, 8).to(torch.bfloat16)
+    img = wp.reshape(npad, cin_pad // 8, 8, 5, 5).flip(3).permute(4, 1, 3, 0, 2).contiguous()
+    return img.to(torch.bfloat16)
 
 
 def dgrad_image(w, cin_pad: int, npad: int):

@@ -9,15 +9,22 @@
 // is a 16-byte move of the operand start address.
 //
 // Forward / data-gradient kernel (conv_fwd_kernel): one CTA owns a 128-site
-// window of a row range. GEMM per output row: M = 128 sites, N = Cout (16 or
-// 32), K = 25 taps x Cin, issued as 25 x Cin/16 MMAs of 128 x N x 16 with the A
-// operand read straight from the staged input rows (K-major, LBO = one channel
-// chunk plane, SBO = 8 sites). Warp 0 stages input rows into a ring with bulk
-// copies (periodic wrap in both axes), warp 1 issues the MMAs into one of two
-// TMEM accumulators, warps 2-5 run the epilogue (bias, GELU, its derivative, or
-// FP32 output) and store. The data gradient of a circular convolution is the
-// forward convolution with the kernel flipped and the channel roles swapped, so
-// the same kernel serves it with the GELU-derivative epilogue.
+// window of up to 16 output rows and stages all of its input rows (the rows plus
+// a 2-row halo above and below, periodic wrap in both axes) in shared memory with
+// bulk copies, one mbarrier per row. Each staged input row, shifted by one of the
+// five x taps, is the A operand (M = 128 sites, K-major, LBO = one channel-chunk
+// plane, SBO = 8 sites) of ONE MMA per 16 input channels whose B operand stacks
+// the five y taps along N (N = 5 x Cout): its five N slices are the contributions
+// of that input row to the five output rows it touches, whose FP32 accumulators
+// sit side by side in TMEM (zeroed first). One 128 x 160 x 16 MMA thus replaces
+// five 128 x 32 x 16 ones and the A tile is read from shared memory once instead
+// of five times. Rows at the edges of the CTA's range issue only the slices of
+// the output rows they own. Warp 0 stages rows, warp 1 issues the MMAs and
+// commits one mbarrier per finished output row, warps 2-9 zero TMEM and then run
+// the epilogue (bias, GELU, its derivative, or FP32 output). The data gradient of
+// a circular convolution is the forward convolution with the kernel flipped and
+// the channel roles swapped, so the same kernel serves it with the
+// GELU-derivative epilogue.
 //
 // Weight-gradient kernel (conv_wgrad_kernel): dW[tap][ci][co] = sum over sites
 // of X[ci][site + tap] dZ[co][site]. Per MMA: M = 128 rows = (ky block, ci), with
@@ -44,8 +51,10 @@ namespace
     constexpr int kTile = 128;              // output sites per tile (one row window)
     constexpr int kSites = kTile + 4;       // staged input sites per row (halo 2 on each side)
     constexpr int kRowPlane = kSites * 16;  // bytes of one channel chunk of one staged row
-    constexpr int kRing = 6;                // staged input rows (forward kernel)
-    constexpr int kThreads = 192;           // warp 0 loads, warp 1 issues MMAs, warps 2-5 epilogue
+    constexpr int kThreads = 192;           // wgrad: warp 0 loads, warp 1 issues MMAs, warps 2-5 epilogue
+    constexpr int kFwdThreads = 320;        // forward: warp 0 loads, warp 1 issues MMAs, warps 2-9 epilogue
+    constexpr int kMaxFwdRows = 16;         // forward: most output rows per CTA (all inputs staged at once)
+    constexpr uint32_t kSmemLimit = 227u * 1024u;
     constexpr int kTaps = 25;
 
     enum Epilogue
@@ -58,7 +67,7 @@ namespace
     struct FwdArgs
     {
         const uint16_t* in;     // [batch][cin/8][nrows][ncols][8]
-        const uint16_t* wimg;   // [25][cin/8][npad][8] (B operand image, K-major)
+        const uint16_t* wimg;   // [5 kx][cin/8][5 (4 - ky)][npad][8] (B operand image, K-major)
         const float* bias;      // [npad] or null
         uint16_t* out;          // [batch][npad/8][nrows][ncols][8]
         uint16_t* pre;          // optional, same layout as out
@@ -80,12 +89,23 @@ namespace
     __host__ __device__ constexpr uint32_t align128(uint32_t x) { return (x + 127u) & ~127u; }
 
     __host__ __device__ inline uint32_t fwd_weight_bytes(int cc, int npad) { return uint32_t(kTaps) * cc * npad * 16u; }
-    __host__ __device__ inline uint32_t fwd_ring_offset(int cc, int npad) { return align128(fwd_weight_bytes(cc, npad)); }
-    __host__ __device__ inline uint32_t fwd_bar_offset(int cc, int npad)
+    __host__ __device__ inline uint32_t fwd_rows_offset(int cc, int npad) { return align128(fwd_weight_bytes(cc, npad)); }
+    __host__ __device__ inline uint32_t fwd_bar_offset(int cc, int npad, int rows)
     {
-        return fwd_ring_offset(cc, npad) + uint32_t(kRing) * cc * kRowPlane;
+        return fwd_rows_offset(cc, npad) + uint32_t(rows + 4) * cc * kRowPlane;
     }
-    __host__ __device__ inline uint32_t fwd_smem_bytes(int cc, int npad) { return fwd_bar_offset(cc, npad) + 256u; }
+    // barriers: full[rows + 4], accf[rows], zero, wbar, done; then the TMEM slot and abort flag
+    __host__ __device__ inline uint32_t fwd_smem_bytes(int cc, int npad, int rows)
+    {
+        return fwd_bar_offset(cc, npad, rows) + uint32_t(2 * rows + 4 + 3) * 8u + 16u;
+    }
+    // TMEM columns: one npad-wide accumulator per output row, rounded up to a power of two
+    __host__ __device__ inline uint32_t fwd_tmem_cols(int npad, int rows)
+    {
+        uint32_t need = uint32_t(npad * rows), c = 32;
+        while (c < need) c <<= 1;
+        return c;
+    }
 
     // wgrad: ky blocks per MMA along M, staged X rows per output-row range
     __host__ __device__ inline int wg_kb(int cc) { return 16 / cc; }
@@ -117,14 +137,27 @@ namespace
         return r < 0 ? r + n : r;
     }
 
+    // GELU in its tanh form (Hendrycks and Gimpel): 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))),
+    // with tanh(u) = 1 - 2 / (exp(2u) + 1) (saturates correctly at both ends).
+    constexpr float kGeluC0 = 0.7978845608028654f;  // sqrt(2 / pi)
+    constexpr float kGeluC1 = 0.044715f;
+
+    __device__ __forceinline__ float tanh_via_exp(float u)
+    {
+        return 1.f - __fdividef(2.f, __expf(2.f * u) + 1.f);
+    }
+
     __device__ __forceinline__ float gelu_f(float z)
     {
-        return 0.5f * z * (1.f + erff(z * 0.70710678118654752f));
+        const float t = tanh_via_exp(kGeluC0 * z * (1.f + kGeluC1 * z * z));
+        return 0.5f * z * (1.f + t);
     }
 
     __device__ __forceinline__ float gelu_grad_f(float z)
     {
-        return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * __expf(-0.5f * z * z);
+        const float z2 = z * z;
+        const float t = tanh_via_exp(kGeluC0 * z * (1.f + kGeluC1 * z2));
+        return 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * kGeluC0 * (1.f + 3.f * kGeluC1 * z2);
     }
 
     __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
@@ -237,49 +270,41 @@ namespace
     }
 
     // ============================================================== forward
-    __global__ void __launch_bounds__(kThreads) conv_fwd_kernel(const FwdArgs a)
+    __global__ void __launch_bounds__(kFwdThreads, 1) conv_fwd_kernel(const FwdArgs a)
     {
         extern __shared__ __align__(1024) uint8_t smem[];
-        const int cc = a.cin_chunks, npad = a.npad;
+        const int cc = a.cin_chunks, npad = a.npad, R = a.rows_per_cta;
         const uint32_t wbytes = fwd_weight_bytes(cc, npad);
         const uint32_t slot_bytes = uint32_t(cc) * kRowPlane;
+        const uint32_t tcols = fwd_tmem_cols(npad, R);
         uint8_t* wsm = smem;
-        uint8_t* ring = smem + fwd_ring_offset(cc, npad);
-        uint64_t* bars = reinterpret_cast<uint64_t*>(smem + fwd_bar_offset(cc, npad));
-        uint64_t* full = bars;
-        uint64_t* empty = bars + kRing;
-        uint64_t* accf = bars + 2 * kRing;
-        uint64_t* acce = accf + 2;
-        uint64_t* wbar = acce + 2;
+        uint8_t* rows = smem + fwd_rows_offset(cc, npad);
+        uint64_t* full = reinterpret_cast<uint64_t*>(smem + fwd_bar_offset(cc, npad, R));
+        uint64_t* accf = full + R + 4;
+        uint64_t* zbar = accf + R;
+        uint64_t* wbar = zbar + 1;
         uint64_t* done = wbar + 1;
         uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
         volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
 
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
         const int nwin = a.ncols / kTile;
-        const int ngroups = (a.nrows + a.rows_per_cta - 1) / a.rows_per_cta;
+        const int ngroups = (a.nrows + R - 1) / R;
         int t = blockIdx.x;
         const int cw = t % nwin;
         t /= nwin;
         const int rg = t % ngroups;
         const int b = t / ngroups;
         const int c0 = cw * kTile;
-        const int r0 = rg * a.rows_per_cta;
-        const int nout = min(a.rows_per_cta, a.nrows - r0);
+        const int r0 = rg * R;
+        const int nout = min(R, a.nrows - r0);
         const int nin = nout + 4;
 
         if (threadIdx.x == 0)
         {
-            for (int i = 0; i < kRing; ++i)
-            {
-                mbar_init(&full[i], 1);
-                mbar_init(&empty[i], 1);
-            }
-            for (int i = 0; i < 2; ++i)
-            {
-                mbar_init(&accf[i], 1);
-                mbar_init(&acce[i], 128);
-            }
+            for (int i = 0; i < R + 4; ++i) mbar_init(&full[i], 1);
+            for (int i = 0; i < R; ++i) mbar_init(&accf[i], 1);
+            mbar_init(zbar, 256);
             mbar_init(wbar, 1);
             mbar_init(done, 1);
             *abort = 0;
@@ -287,7 +312,7 @@ namespace
         }
         if (warp == 0)
         {
-            tmem_alloc(tslot, 64);
+            tmem_alloc(tslot, tcols);
             tmem_relinquish();
         }
         tc_fence_before();
@@ -299,80 +324,67 @@ namespace
         {
             if (lane == 0)
             {
+                // every input row of this CTA at once, one mbarrier per row, in the order
+                // the MMAs consume them
                 mbar_expect_tx(wbar, wbytes);
                 bulk_g2s(wsm, a.wimg, wbytes, wbar);
-                int issued = 0;
                 const int cl = (c0 - 2 + a.ncols) % a.ncols;
                 const int cr = (c0 + kTile) % a.ncols;
                 for (int i = 0; i < nin; ++i)
                 {
-                    const int s = i % kRing;
-                    if (i >= kRing && !mbar_wait(&empty[s], ((i / kRing) - 1) & 1, abort))
-                    {
-                        give_up(a.error, abort, 1);
-                        break;
-                    }
                     const int row = wrap_row(r0 - 2 + i, a.nrows);
-                    mbar_expect_tx(&full[s], slot_bytes);
-                    uint8_t* dst = ring + s * slot_bytes;
+                    mbar_expect_tx(&full[i], slot_bytes);
+                    uint8_t* dst = rows + i * slot_bytes;
                     for (int q = 0; q < cc; ++q)
                     {
                         const uint16_t* src = a.in + (size_t(b * cc + q) * a.nrows + row) * size_t(a.ncols) * 8;
                         uint8_t* d = dst + q * kRowPlane;
-                        bulk_g2s(d, src + size_t(cl) * 8, 32, &full[s]);
-                        bulk_g2s(d + 32, src + size_t(c0) * 8, kTile * 16, &full[s]);
-                        bulk_g2s(d + 32 + kTile * 16, src + size_t(cr) * 8, 32, &full[s]);
+                        bulk_g2s(d, src + size_t(cl) * 8, 32, &full[i]);
+                        bulk_g2s(d + 32, src + size_t(c0) * 8, kTile * 16, &full[i]);
+                        bulk_g2s(d + 32 + kTile * 16, src + size_t(cr) * 8, 32, &full[i]);
                     }
-                    issued = i + 1;
                 }
                 // no copy may still be in flight when the CTA exits
                 mbar_wait(wbar, 0, nullptr);
-                for (int i = issued > kRing ? issued - kRing : 0; i < issued; ++i)
-                    mbar_wait(&full[i % kRing], (i / kRing) & 1, nullptr);
+                for (int i = 0; i < nin; ++i) mbar_wait(&full[i], 0, nullptr);
             }
         }
         else if (warp == 1)
         {
             if (lane == 0)
             {
-                const uint32_t idesc = idesc_bf16(128, npad, false, false);
-                const uint32_t wsa = smem_u32(wsm), rsa = smem_u32(ring);
-                bool ok = mbar_wait(wbar, 0, abort);
+                const uint32_t wsa = smem_u32(wsm), rsa = smem_u32(rows);
+                const uint32_t kblock = 5u * npad * 16u;  // one (x tap, channel chunk) block of the image
+                bool ok = mbar_wait(wbar, 0, abort) && mbar_wait(zbar, 0, abort);
+                tc_fence_after();
                 bool issued_any = false;
-                for (int j = 0; ok && j < nout; ++j)
+                for (int i = 0; ok && i < nin; ++i)
                 {
-                    const int acc = j & 1;
-                    if (j >= 2 && !mbar_wait(&acce[acc], ((j >> 1) - 1) & 1, abort))
+                    if (!mbar_wait(&full[i], 0, abort))
                     {
                         ok = false;
                         break;
                     }
-                    tc_fence_after();
-                    const uint32_t d = tbase + uint32_t(acc * npad);
-                    uint32_t accumulate = 0;
-                    for (int ky = 0; ky < 5 && ok; ++ky)
+                    // slice s of this row's MMA feeds output row i - 4 + s (y tap 4 - s)
+                    const int s_lo = i < 4 ? 4 - i : 0;
+                    const int s_hi = nout + 3 - i < 4 ? nout + 3 - i : 4;
+                    if (s_lo <= s_hi)
                     {
-                        const int i = j + ky, s = i % kRing;
-                        if (!mbar_wait(&full[s], (i / kRing) & 1, abort))
-                        {
-                            ok = false;
-                            break;
-                        }
-                        const uint32_t sa = rsa + s * slot_bytes;
+                        const int n = npad * (s_hi - s_lo + 1);
+                        const uint32_t idesc = idesc_bf16(128, n, false, false);
+                        const uint32_t d = tbase + uint32_t((i - 4 + s_lo) * npad);
+                        const uint32_t sa = rsa + i * slot_bytes;
                         for (int kx = 0; kx < 5; ++kx)
                             for (int ks = 0; ks < cc / 2; ++ks)
                             {
                                 const uint64_t ad = smem_desc(sa + 2 * ks * kRowPlane + kx * 16, kRowPlane, 128);
-                                const uint64_t bd =
-                                    smem_desc(wsa + ((ky * 5 + kx) * cc + 2 * ks) * npad * 16, npad * 16, 128);
-                                mma_bf16(d, ad, bd, idesc, accumulate);
-                                accumulate = 1;
+                                const uint64_t bd = smem_desc(
+                                    wsa + (kx * cc + 2 * ks) * kblock + uint32_t(s_lo * npad * 16), kblock, 128);
+                                mma_bf16(d, ad, bd, idesc, 1u);
                                 issued_any = true;
                             }
                     }
-                    if (!ok) break;
-                    mma_commit(&accf[acc]);
-                    mma_commit(&empty[j % kRing]);
+                    if (i >= 4) mma_commit(&accf[i - 4]);  // output row i - 4 has all five y taps
                 }
                 if (!ok) give_up(a.error, abort, 2);
                 if (issued_any)
@@ -384,14 +396,31 @@ namespace
         }
         else
         {
-            const int q4 = warp & 3;  // the TMEM lane quarter this warp may read
+            // warps 2-9: lane quarter (warp % 4) of the tile, column half (warp - 2) / 4
+            const int q4 = warp & 3;  // the TMEM lane quarter this warp may access
+            const int half = (warp - 2) >> 2;
             const int m = q4 * 32 + lane;
             const int col = c0 + m;
             const int nq = npad / 8;
+            const bool active = half * 16 < npad;  // npad 16: the second half has no columns
+            const size_t plane = size_t(a.nrows) * a.ncols;
+            float bias[16];
+#pragma unroll
+            for (int e = 0; e < 16; ++e)
+            {
+                const int n = half * 16 + e;
+                bias[e] = (a.bias && n < npad) ? a.bias[n] : 0.f;
+            }
+            // zero this warp's half of the accumulator columns in its lane quarter
+            const uint32_t lanes = uint32_t(q4 * 32) << 16;
+            for (uint32_t c = half * (tcols / 2); c < (half + 1) * (tcols / 2); c += 16)
+                tmem_st16_zero(tbase + lanes + c);
+            tmem_wait_st();
+            tc_fence_before();
+            mbar_arrive(zbar);
             for (int j = 0; j < nout; ++j)
             {
-                const int acc = j & 1;
-                bool ok = mbar_wait(&accf[acc], (j >> 1) & 1, abort);
+                bool ok = mbar_wait(&accf[j], 0, abort);
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok)
                 {
@@ -399,29 +428,28 @@ namespace
                     break;
                 }
                 tc_fence_after();
+                if (!active) continue;
                 float v[32];
-                const uint32_t taddr = tbase + (uint32_t(q4 * 32) << 16) + uint32_t(acc * npad);
-                if (npad == 32) tmem_ld32(taddr, v);
-                else tmem_ld16(taddr, v);
+                tmem_ld16(tbase + lanes + uint32_t(j * npad + half * 16), v);
                 tmem_wait_ld();
-                tc_fence_before();
-                mbar_arrive(&acce[acc]);
 
                 const int row = r0 + j;
                 const size_t site = size_t(row) * a.ncols + col;
-                const size_t plane = size_t(a.nrows) * a.ncols;
                 if (a.epilogue == EPI_F32)
                 {
 #pragma unroll
-                    for (int n = 0; n < 32; ++n)
-                        if (n < a.cout)
-                            a.out_f32[(size_t(b) * a.cout + n) * plane + site] = v[n] + (a.bias ? a.bias[n] : 0.f);
+                    for (int e = 0; e < 16; ++e)
+                    {
+                        const int n = half * 16 + e;
+                        if (n < a.cout) a.out_f32[(size_t(b) * a.cout + n) * plane + site] = v[e] + bias[e];
+                    }
                 }
                 else
                 {
 #pragma unroll
-                    for (int q = 0; q < 4; ++q)
+                    for (int qq = 0; qq < 2; ++qq)
                     {
+                        const int q = half * 2 + qq;
                         if (q >= nq) break;
                         const size_t off = ((size_t(b) * nq + q) * plane + site) * 8;
                         float o[8];
@@ -431,7 +459,7 @@ namespace
 #pragma unroll
                             for (int e = 0; e < 8; ++e)
                             {
-                                z[e] = v[8 * q + e] + (a.bias ? a.bias[8 * q + e] : 0.f);
+                                z[e] = v[8 * qq + e] + bias[8 * qq + e];
                                 o[e] = gelu_f(z[e]);
                             }
                             if (a.pre)
@@ -444,7 +472,7 @@ namespace
                             float g[8];
                             unpack_bf16x8(*reinterpret_cast<const uint4*>(a.gate + off), g);
 #pragma unroll
-                            for (int e = 0; e < 8; ++e) o[e] = v[8 * q + e] * gelu_grad_f(g[e]);
+                            for (int e = 0; e < 8; ++e) o[e] = v[8 * qq + e] * gelu_grad_f(g[e]);
                         }
                         *reinterpret_cast<uint4*>(a.out + off) =
                             make_uint4(pack_bf16x2(o[0], o[1]), pack_bf16x2(o[2], o[3]), pack_bf16x2(o[4], o[5]),
@@ -459,7 +487,7 @@ namespace
         if (warp == 0)
         {
             tc_fence_after();
-            tmem_dealloc(tbase, 64);
+            tmem_dealloc(tbase, tcols);
         }
     }
 
@@ -745,18 +773,21 @@ namespace
         return g_sms;
     }
 
-    // Rows per CTA for the forward kernel: few waves of two resident CTAs per SM, each
-    // CTA paying a four-row halo.
-    int choose_fwd_rows(int batch, int nrows, int nwin)
+    // Rows per CTA for the forward kernel: every CTA stages all its input rows at once, so
+    // shared memory and TMEM per CTA grow with the rows (at most kMaxFwdRows); one CTA per
+    // SM (320 threads at ~150 registers); cost = waves x (rows + about three row times of
+    // pipeline fill).
+    int choose_fwd_rows(int batch, int nrows, int nwin, int cc, int npad)
     {
-        const int slots = 2 * sm_count();
+        const int sms = sm_count();
         int best = 1;
         double best_cost = 1e30;
-        for (int r = 1; r <= nrows && r <= 64; ++r)
+        for (int r = 1; r <= kMaxFwdRows && r <= nrows; ++r)
         {
+            if (fwd_smem_bytes(cc, npad, r) > kSmemLimit || npad * r > 512) break;
             const long long grid = (long long)batch * nwin * ((nrows + r - 1) / r);
-            const long long waves = (grid + slots - 1) / slots;
-            const double cost = double(waves) * (r + 4);
+            const long long waves = (grid + sms - 1) / sms;
+            const double cost = double(waves) * (r + 3);
             if (cost < best_cost - 1e-9)
             {
                 best_cost = cost;
@@ -768,9 +799,21 @@ namespace
 
     constexpr int kWgradRows = 8;
 
-    cudaError_t set_smem_attr(const void* fn, uint32_t bytes)
+    // Raises a kernel's dynamic shared-memory limit once per device (so that later
+    // launches, e.g. inside a stream capture, make no attribute calls).
+    std::mutex g_attr_mutex;
+    int g_attr_selftest[64], g_attr_fwd[64], g_attr_wgrad[64];
+
+    cudaError_t set_smem_attr(const void* fn, uint32_t bytes, int (&done)[64])
     {
-        return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+        std::lock_guard<std::mutex> lock(g_attr_mutex);
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+        if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = 1;
+        return e;
     }
 
     bool valid_geometry(int batch, int nrows, int ncols)
@@ -800,7 +843,7 @@ extern "C" int amb_tc_selftest(const void* a, const void* b, float* d, int n, in
     if (!a || !b || !d || (n != 16 && n != 32) || k < 16 || k > 64 || k % 16 != 0)
         return fail_invalid("amb_tc_selftest: n must be 16 or 32, k in {16, 32, 48, 64}");
     const uint32_t smem = 98304 + 256;
-    cudaError_t e = set_smem_attr(reinterpret_cast<const void*>(tc_selftest_kernel), smem);
+    cudaError_t e = set_smem_attr(reinterpret_cast<const void*>(tc_selftest_kernel), smem, g_attr_selftest);
     if (e == cudaSuccess)
     {
         tc_selftest_kernel<<<1, 128, smem, static_cast<cudaStream_t>(stream)>>>(
@@ -841,14 +884,14 @@ extern "C" int amb_conv5x5_forward(const void* in, int batch, int nrows, int nco
     a.cout = epilogue == EPI_F32 ? cout : npad;
     a.epilogue = epilogue;
     const int nwin = ncols / kTile;
-    a.rows_per_cta = choose_fwd_rows(batch, nrows, nwin);
+    a.rows_per_cta = choose_fwd_rows(batch, nrows, nwin, a.cin_chunks, npad);
     a.error = error;
-    const uint32_t smem = fwd_smem_bytes(a.cin_chunks, npad);
-    cudaError_t e = set_smem_attr(reinterpret_cast<const void*>(conv_fwd_kernel), fwd_smem_bytes(4, 32));
+    const uint32_t smem = fwd_smem_bytes(a.cin_chunks, npad, a.rows_per_cta);
+    cudaError_t e = set_smem_attr(reinterpret_cast<const void*>(conv_fwd_kernel), kSmemLimit, g_attr_fwd);
     if (e == cudaSuccess)
     {
         const long long grid = (long long)batch * nwin * ((nrows + a.rows_per_cta - 1) / a.rows_per_cta);
-        conv_fwd_kernel<<<unsigned(grid), kThreads, smem, static_cast<cudaStream_t>(stream)>>>(a);
+        conv_fwd_kernel<<<unsigned(grid), kFwdThreads, smem, static_cast<cudaStream_t>(stream)>>>(a);
         e = cudaGetLastError();
     }
     return e == cudaSuccess ? AMB_OK : fail_cuda("amb_conv5x5_forward", e);
@@ -886,7 +929,8 @@ extern "C" int amb_conv5x5_wgrad(const void* x, const void* dz, int batch, int n
     a.error = error;
     const uint32_t smem = wg_smem_bytes(a.cin_chunks, npad, kWgradRows);
     cudaError_t e = set_smem_attr(reinterpret_cast<const void*>(conv_wgrad_kernel),
-                                  std::max(wg_smem_bytes(4, 32, kWgradRows), wg_smem_bytes(2, 32, kWgradRows)));
+                                  std::max(wg_smem_bytes(4, 32, kWgradRows), wg_smem_bytes(2, 32, kWgradRows)),
+                                  g_attr_wgrad);
     auto s = static_cast<cudaStream_t>(stream);
     const long long grid = wgrad_grid(batch, nrows, ncols);
     if (e == cudaSuccess)

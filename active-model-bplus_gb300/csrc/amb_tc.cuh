@@ -167,6 +167,22 @@ namespace tc
         for (int i = 16; i < 32; ++i) v[i] = 0.f;
     }
 
+    // Each thread of the warp writes zeros to 16 consecutive columns of its own TMEM lane.
+    __device__ __forceinline__ void tmem_st16_zero(uint32_t taddr)
+    {
+        const uint32_t z = 0u;
+        asm volatile(
+            "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+            "%1, %1};" ::"r"(taddr),
+            "r"(z)
+            : "memory");
+    }
+
+    __device__ __forceinline__ void tmem_wait_st()
+    {
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+    }
+
     __device__ __forceinline__ void tmem_wait_ld()
     {
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");

@@ -237,8 +237,8 @@ int amb_label_components_f32(const float* field, int nrows, int ncols, double th
  * Activations are bf16 "chunk planes": [batch][C/8][nrows][ncols][8] (16-byte
  * aligned). Requirements: ncols % 128 == 0, nrows >= 3, C in {16, 32}.
  * Convolution weights are passed as a bf16 B-operand image
- * [25 taps (ky*5+kx)][Cin/8][npad][8]: element (tap, ci, co) at
- * ((tap*Cin/8 + ci/8)*npad + co)*8 + ci%8, co < npad zero-padded.
+ * [5 (kx)][Cin/8][5 (4 - ky)][npad][8]: element (ky, kx, ci, co) at
+ * (((kx*Cin/8 + ci/8)*5 + 4 - ky)*npad + co)*8 + ci%8, co < npad zero-padded.
  * *error (device int, may be NULL) receives a non-zero code if a kernel gave up
  * waiting on its own pipeline (the outputs are then incomplete). */
 
@@ -249,7 +249,7 @@ int amb_tc_selftest(const void* a, const void* b, float* d, int n, int k, int a_
                     void* stream);
 
 /* Epilogues of amb_conv5x5_forward */
-#define AMB_EPI_GELU 0     /* out = bf16(gelu(acc + bias)); pre (optional) = bf16(acc + bias) */
+#define AMB_EPI_GELU 0     /* out = bf16(gelu(acc + bias)) (tanh-form GELU); pre (optional) = bf16(acc + bias) */
 #define AMB_EPI_F32 1      /* out_f32[batch][cout][nrows][ncols] = acc + bias (first cout channels) */
 #define AMB_EPI_GELU_BWD 2 /* out = bf16(acc * gelu'(gate)), gate = pre-activation, same layout as out */
 

@@ -8,7 +8,7 @@ has no learned component), so its oracle is the mathematics it implements:
   defines it) over periodically padded input, evaluated by torch on the CPU in
   float64;
 * its data and weight gradients (torch autograd in float64);
-* GELU with the exact erf form and its derivative;
+* GELU in its tanh form (Hendrycks and Gimpel) and its derivative;
 * the face-flux update in int64 fixed point (phi * 2^24), restated with the
   same IEEE double operations as the device kernel (product, then round half to
   even), so it is bit-exact at T = 0;
@@ -63,16 +63,20 @@ def conv5x5_grads(x, w, dout):
     return xt.grad.numpy(), wt.grad.numpy()
 
 
+GELU_C0 = math.sqrt(2.0 / math.pi)
+GELU_C1 = 0.044715
+
+
 def gelu(z):
+    """GELU in its tanh form (Hendrycks and Gimpel), as the device epilogue evaluates it."""
     z = np.asarray(z, dtype=np.float64)
-    from scipy.special import erf
-    return 0.5 * z * (1.0 + erf(z / math.sqrt(2.0)))
+    return 0.5 * z * (1.0 + np.tanh(GELU_C0 * (z + GELU_C1 * z ** 3)))
 
 
 def gelu_grad(z):
     z = np.asarray(z, dtype=np.float64)
-    from scipy.special import erf
-    return 0.5 * (1.0 + erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+    t = np.tanh(GELU_C0 * (z + GELU_C1 * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * GELU_C0 * (1.0 + 3.0 * GELU_C1 * z * z)
 
 
 def network_input(phi, params):

@@ -13,18 +13,31 @@ from activemodelbplus import learned as L
 
 
 def emulate_conv(xc, img, npad):
-    """What amb_conv5x5_forward computes, from the same buffers: for output site (r, c),
-    tap (ky, kx) reads staged site m + kx of input row r + ky - 2 (A operand, K-major over
-    the channel chunks) against image[tap][chunk][co][e] (B operand)."""
+    """What amb_conv5x5_forward computes, from the same buffers: input row i shifted by
+    x tap kx (A operand, K-major over the channel chunks) times image[kx][chunk][s][co][e]
+    (B operand, N = (s, co)) adds slice s to output row i - 4 + s, i.e. y tap ky = 4 - s."""
     xc = xc.float().numpy().astype(np.float64)      # [B, q, H, W, 8]
-    im = img.float().numpy().astype(np.float64)     # [25, q, npad, 8]
+    im = img.float().numpy().astype(np.float64)     # [5 kx, q, 5 s, npad, 8]
     B, q, H, W, _ = xc.shape
     out = np.zeros((B, npad, H, W))
     for ky in range(5):
         for kx in range(5):
             xs = np.roll(xc, shift=(-(ky - 2), -(kx - 2)), axis=(2, 3))  # xs[r, c] = x[r+ky-2, c+kx-2]
-            out += np.einsum("bqhwe,qne->bnhw", xs, im[ky * 5 + kx])
+            out += np.einsum("bqhwe,qne->bnhw", xs, im[kx][:, 4 - ky])
     return out
+
+
+def emulate_row_slices(nout):
+    """The forward kernel's MMA schedule for one CTA of nout output rows: input row i
+    (0 <= i < nout + 4) issues slices s_lo..s_hi, slice s feeding output row i - 4 + s with
+    y tap 4 - s. Returns the (output row, y tap) pairs covered."""
+    seen = []
+    for i in range(nout + 4):
+        s_lo = 4 - i if i < 4 else 0
+        s_hi = min(nout + 3 - i, 4)
+        for s in range(s_lo, s_hi + 1):
+            seen.append((i - 4 + s, 4 - s))
+    return seen
 
 
 def emulate_wgrad(xc, dzc):
@@ -90,6 +103,12 @@ def test_wgrad_output_order(cin, cin_used, npad, cout):
     _, dw_ref = OL.conv5x5_grads(OL.bf16_round(x.numpy()), np.zeros((cout, cin_used, 5, 5)),
                                  OL.bf16_round(dz.numpy()))
     assert np.abs(got - dw_ref).max() < 1e-9 * max(1.0, np.abs(dw_ref).max())
+
+
+@pytest.mark.parametrize("nout", [1, 2, 3, 4, 5, 7, 16])
+def test_forward_slices_cover_every_tap_once(nout):
+    seen = emulate_row_slices(nout)
+    assert sorted(seen) == [(o, ky) for o in range(nout) for ky in range(5)]
 
 
 def test_d8_face_sums_reproduce_the_central_difference():
