@@ -177,10 +177,15 @@ class Integrator:
             like the reference's non-deterministic seed.
         device: CUDA device (default: current).
         kernel: "auto", "tile" or "sliding" (FP32 kernel choice).
+        autotune: with kernel="auto" and FP32 storage, time the candidate kernels and
+            launch shapes for this grid once per process (``amb_autotune_f32``) and use
+            the fastest; otherwise a shape heuristic decides. The two FP32 kernels agree
+            to FP32 rounding, not bitwise; name a kernel for bitwise reproducibility
+            across processes.
     """
 
     def __init__(self, field, stencil, model, *, precision: str = "f64", seed: int | None = None,
-                 device=None, kernel: str = "auto"):
+                 device=None, kernel: str = "auto", autotune: bool = True):
         torch = _torch()
         if not torch.cuda.is_available():
             raise CudaException("no CUDA device is available")
@@ -216,11 +221,25 @@ class Integrator:
         self._s = N.stencil_struct(self._stencil)
         self._m = N.model_struct(self._model)
         self.set_field(host)
+        self._tuned = None
+        if autotune and kernel == "auto" and precision != "f64":
+            cfg, us = N.amb_kernel_config(), ctypes.c_double()
+            _check(lib.amb_autotune_f32(ctypes.byref(self._s), ctypes.byref(self._m), self._ny, self._nx,
+                                        int(precision == "f32c"), 8, self._stream(), ctypes.byref(cfg),
+                                        ctypes.byref(us)))
+            names = {N.AMB_KERNEL_TILE: "tile", N.AMB_KERNEL_SLIDING: "sliding"}
+            self._tuned = {"kernel": names.get(cfg.kernel, "auto"), "seg_rows": cfg.seg_rows,
+                           "pairs_per_cta": cfg.pairs_per_cta, "us_per_step": us.value}
         del lib
 
     # -------------------------------------------------------------- plumbing
     def _stream(self) -> int:
         return _torch().cuda.current_stream(self._device).cuda_stream
+
+    @property
+    def kernel_config(self):
+        """The autotuned FP32 kernel configuration (dict) or None."""
+        return None if self._tuned is None else dict(self._tuned)
 
     @property
     def field_tensor(self):

@@ -69,6 +69,8 @@ SIGNATURES = {
     "amb_step_f32": (_I, [_SP, _MP, _U64, _I, _I, _VP, _VP, _VP, _I64, _I, _VP, _I, _VP, _IP]),
     "amb_step_f32_ex": (_I, [_SP, _MP, _U64, _I, _I, _VP, _VP, _VP, _I64, _I, _VP, ctypes.POINTER(amb_kernel_config),
                              _VP, _IP]),
+    "amb_autotune_f32": (_I, [_SP, _MP, _I, _I, _I, _I, _VP, ctypes.POINTER(amb_kernel_config),
+                              ctypes.POINTER(ctypes.c_double)]),
     "amb_terms_f64": (_I, [_SP, _MP, _U64, _I, _I, _VP, _I64, _VP, _VP, _VP]),
     "amb_terms_f32": (_I, [_SP, _MP, _U64, _I, _I, _VP, _I64, _VP, _VP, _VP]),
     "amb_mass_scratch_bytes": (ctypes.c_size_t, [_I64]),
@@ -93,8 +95,9 @@ SIGNATURES = {
     "amb_conv5x5_wgrad_scratch_bytes": (ctypes.c_size_t, [_I, _I, _I, _I, _I]),
     "amb_conv5x5_wgrad": (_I, [_VP, _VP, _I, _I, _I, _I, _I, _VP, _VP, ctypes.c_size_t, _VP, _VP]),
     "amb_learned_input": (_I, [_VP, _VP, _I, _I, _I, _VP, _VP]),
-    "amb_learned_update": (_I, [_VP, _I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
-                                _U64, _VP, _VP, _VP, _VP, ctypes.c_double, _VP, _VP]),
+    "amb_learned_noise": (_I, [_I, _I, _U64, _VP, _VP, _VP]),
+    "amb_learned_update": (_I, [_VP, _I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, _VP,
+                                ctypes.c_double, _VP, _VP, ctypes.c_double, _VP, _VP]),
 }
 
 _lib = None

@@ -1,7 +1,9 @@
 """Learned coarse stepper (no reference counterpart).
 
 A periodic convolutional network maps (phi, zeta, lambda, T) to a face flux F
-that advances the field by K explicit-Euler steps at once:
+that, added to the exact flux of the scheme's stiff linear part (``LinearPart``,
+the K-step propagator of the scheme linearised about the bulk, applied with FFTs),
+advances the field by K explicit-Euler steps at once:
 
     phi(t + K dt) = phi(t) - K dt * div F  (+ the K-step noise flux when T > 0)
 
@@ -12,8 +14,8 @@ weights and activations with FP32 accumulation; its forward and both backward
 passes run on this package's own tcgen05 implicit-GEMM kernels
 (``amb_conv5x5_forward`` / ``amb_conv5x5_wgrad``). Training targets are the
 deterministic K-step increments of the plain integrator started from states of
-noisy trajectories; the noise is added back per macro step as the exact K-step
-aggregate of the plain scheme's noise flux. The plain integrator is the
+noisy trajectories; the noise of a macro step is one Philox draw shaped per Fourier
+mode by the K-step accumulation of the linearised plain scheme (``noise_filter``). The plain integrator is the
 fallback: every ``check_every`` macro steps one step is compared with K plain
 deterministic steps from the same state, and if the residual exceeds ``tol``
 (or the field left its bounds) the span since the last check is redone with
@@ -172,6 +174,7 @@ class FluxNet:
             self.weights.append((torch.randn(self.cout[l], self.cin_used[l], 5, 5, generator=g) * std).to(device))
             self.biases.append(torch.zeros(self.npad[l], device=device))
         self.error = torch.zeros(1, dtype=torch.int32, device=device)
+        self.linear_split = True  # the network predicts the flux beyond the exact linear part
         self._images = None
         self._dimages = None
         self._saved = None
@@ -191,6 +194,7 @@ class FluxNet:
         for l in range(NLAYERS):
             d[f"w{l}"] = self.weights[l].cpu().numpy()
             d[f"b{l}"] = self.biases[l].cpu().numpy()
+        d["linear_split"] = np.asarray(int(self.linear_split))
         return d
 
     def load_state_dict(self, d) -> None:
@@ -198,6 +202,7 @@ class FluxNet:
         for l in range(NLAYERS):
             self.weights[l] = torch.as_tensor(np.asarray(d[f"w{l}"]), dtype=torch.float32).to(self.device)
             self.biases[l] = torch.as_tensor(np.asarray(d[f"b{l}"]), dtype=torch.float32).to(self.device)
+        self.linear_split = bool(int(np.asarray(d["linear_split"]))) if "linear_split" in d else False
         self._images = None
 
     def save(self, path: str, **meta) -> None:
@@ -320,13 +325,34 @@ def generate_pairs(n_traj: int, size: int, K: int, sample_steps, *, dt: float = 
     return phi, delta, model_params_tensor(models, "cuda"), models
 
 
+def lowpass_weights(shape, sigma: float, device=None):
+    """Gaussian low-pass exp(-sigma^2 |k|^2 / 2) per rfft2 mode (k in radians per site)."""
+    torch = _torch()
+    ny, nx = shape
+    ky = 2 * np.pi * np.fft.fftfreq(ny)[:, None]
+    kx = 2 * np.pi * np.fft.rfftfreq(nx)[None, :]
+    w = np.exp(-0.5 * sigma * sigma * (kx * kx + ky * ky)).astype(np.float32)
+    return torch.from_numpy(w).to(device if device is not None else "cuda")
+
+
+def lowpass(x, w):
+    """Apply rfft2-layout weights w to the last two dimensions of x (cuFFT through torch)."""
+    torch = _torch()
+    return torch.fft.irfft2(torch.fft.rfft2(x) * w, s=x.shape[-2:])
+
+
 def train(net: FluxNet, phi, delta, params, *, K: int, dt: float, iters: int, batch: int = 16, lr: float = 2e-3,
-          seed: int = 0, log_every: int = 0):
+          seed: int = 0, log_every: int = 0, lowpass_sigma: float = 0.0, highpass_weight: float = 1.0,
+          linear: LinearPart | None = None):
     """Fit the flux so that -K dt div F matches the deterministic K-step increments.
 
     phi, delta: [S, n, H, W]; params: [n, 3]. Adam on the FP32 master weights; the
-    gradients come from the network's own backward kernels. Returns the loss history
-    (relative mean-square error per iteration).
+    gradients come from the network's own backward kernels. With lowpass_sigma > 0 the
+    loss is the relative mean-square error of the Gaussian-low-passed increments (the
+    slow, large-scale dynamics that set domain sizes) plus highpass_weight times the plain
+    relative MSE; otherwise the plain relative MSE. With ``linear`` (and net.linear_split)
+    the predicted increment is that of the network's flux plus the exact linear part's.
+    Returns the loss history.
     """
     torch = _torch()
     S, n, H, W = phi.shape
@@ -338,16 +364,23 @@ def train(net: FluxNet, phi, delta, params, *, K: int, dt: float, iters: int, ba
     sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, T_max=max(1, iters), eta_min=lr * 0.05)
     dtk = K * dt
     scale = float(delta.square().mean().item()) + 1e-30
+    wlp = lowpass_weights((H, W), lowpass_sigma, phi.device) if lowpass_sigma > 0 else None
+    scale_lp = 1.0
+    if wlp is not None:
+        scale_lp = sum(float(lowpass(delta[k], wlp).square().mean().item()) for k in range(S)) / S + 1e-30
     hist = []
     for it in range(iters):
-        si = torch.randint(0, S, (batch,), generator=g)
-        ni = torch.randint(0, n, (batch,), generator=g)
-        si, ni = si.to(phi.device), ni.to(phi.device)
+        si = torch.randint(0, S, (batch,), generator=g).to(phi.device)
+        ni = torch.randint(0, n, (batch,), generator=g).to(phi.device)
         x = network_input(phi[si, ni].contiguous(), params[ni].contiguous())
         flux = net.forward(x, train=True)
         f = flux.detach().requires_grad_(True)
-        pred = -dtk * divergence(f, 1.0, 1.0)
-        loss = (pred - delta[si, ni]).square().mean() / scale
+        total = f if linear is None else f + linear.flux(phi[si, ni])
+        r = -dtk * divergence(total, 1.0, 1.0) - delta[si, ni]
+        if wlp is None:
+            loss = r.square().mean() / scale
+        else:
+            loss = lowpass(r, wlp).square().mean() / scale_lp + highpass_weight * r.square().mean() / scale
         loss.backward()
         gw, gb = net.backward(f.grad)
         for p, gr in zip(params_list, gw + gb):
@@ -361,40 +394,135 @@ def train(net: FluxNet, phi, delta, params, *, K: int, dt: float, iters: int, ba
     return hist
 
 
-def evaluate(net: FluxNet, phi, delta, params, *, K: int, dt: float, batch: int = 16):
-    """Relative mean-square error of the predicted K-step increments over a pair set."""
-    torch = _torch()
+def evaluate(net: FluxNet, phi, delta, params, *, K: int, dt: float, batch: int = 16, lowpass_sigma: float = 0.0,
+             linear: LinearPart | None = None):
+    """Relative mean-square error of the predicted K-step increments over a pair set
+    (of their Gaussian low-passed versions when lowpass_sigma > 0)."""
     S, n, H, W = phi.shape
+    wlp = lowpass_weights((H, W), lowpass_sigma, phi.device) if lowpass_sigma > 0 else None
     num, den = 0.0, 0.0
     flat_phi = phi.reshape(S * n, H, W)
     flat_delta = delta.reshape(S * n, H, W)
     flat_params = params.repeat(S, 1)
     for i in range(0, S * n, batch):
         x = network_input(flat_phi[i:i + batch].contiguous(), flat_params[i:i + batch].contiguous())
-        pred = -K * dt * divergence(net.forward(x), 1.0, 1.0)
-        num += float((pred - flat_delta[i:i + batch]).square().sum().item())
-        den += float(flat_delta[i:i + batch].square().sum().item())
+        flux = net.forward(x)
+        if linear is not None:
+            flux = flux + linear.flux(flat_phi[i:i + batch])
+        pred = -K * dt * divergence(flux, 1.0, 1.0)
+        ref = flat_delta[i:i + batch]
+        if wlp is not None:
+            pred, ref = lowpass(pred, wlp), lowpass(ref, wlp)
+        num += float((pred - ref).square().sum().item())
+        den += float(ref.square().sum().item())
     return num / max(den, 1e-30)
 
 
 # -------------------------------------------------------------- stepper
 
+def bulk_curvature(model) -> float:
+    """f''(phi) in the bulk phases: -2a for the symmetric double well a < 0 < c (b = 0), else a."""
+    m = Model(model)
+    return -2.0 * m.a if (m.a < 0 and m.c > 0) else m.a
+
+
+def linear_rate(shape, stencil, model, curvature: float | None = None) -> np.ndarray:
+    """Decay rate w(k) (rfft2 layout [ny, nx//2 + 1]) of the plain scheme linearised about a
+    uniform state with free-energy curvature f'': w = (s_x^2 + s_y^2)(f'' - kappa L(k)), with s
+    the symbol of the order-8 first derivative and L that of the Tjhung Laplacian."""
+    ny, nx = shape
+    st, m = Stencil(stencil), Model(model)
+    f2 = bulk_curvature(m) if curvature is None else curvature
+    ty = 2 * np.pi * np.fft.fftfreq(ny)[:, None]
+    tx = 2 * np.pi * np.fft.rfftfreq(nx)[None, :]
+    c = (4.0 / 5.0, -1.0 / 5.0, 4.0 / 105.0, -1.0 / 280.0)
+    sx = (2.0 / st.dx) * sum(cd * np.sin((d + 1) * tx) for d, cd in enumerate(c))
+    sy = (2.0 / st.dy) * sum(cd * np.sin((d + 1) * ty) for d, cd in enumerate(c))
+    lap = ((1.5 - 0.5 * np.cos(ty)) * (2 * np.cos(tx) - 2) / st.dx ** 2 +
+           (1.5 - 0.5 * np.cos(tx)) * (2 * np.cos(ty) - 2) / st.dy ** 2)
+    return (sx ** 2 + sy ** 2) * (f2 - m.kappa * lap)
+
+
+def noise_filter(shape, stencil, model, K: int, curvature: float | None = None):
+    """Per-mode amplitude factor g(k) (rfft2 layout) that turns one draw of the K-step noise
+    flux into the noise the linearised plain scheme accumulates over K steps: one step maps
+    a mode by a(k) = 1 - dt w(k), so K steps of independent noise add sum_j a^(2j) =
+    (1 - a^(2K)) / (1 - a^2) times the one-step variance, where a single macro draw adds K
+    times it: g^2 = (1 - a^(2K)) / (K (1 - a^2))."""
+    torch = _torch()
+    a = 1.0 - Stencil(stencil).dt * linear_rate(shape, stencil, model, curvature)
+    one_minus = 1.0 - a * a
+    with np.errstate(divide="ignore", invalid="ignore"):
+        g2 = np.where(np.abs(one_minus) > 1e-12, (1.0 - a ** (2 * K)) / (K * one_minus), 1.0)
+    return torch.from_numpy(np.sqrt(np.clip(g2, 0.0, None)).astype(np.float32))
+
+
+class LinearPart:
+    """The stiff linear part of K plain steps, applied exactly and written as a face flux.
+
+    K explicit steps of the scheme linearised about the bulk multiply mode k by
+    E(k) = a(k)^K. The face flux G with (face-difference) divergence
+    div G = -(E - 1) phi / (K dt) is G_hat = -(E - 1) phi_hat conj(d) / (|d_x|^2 + |d_y|^2) / (K dt)
+    per component, d_x = (1 - exp(-i k_x dx)) / dx the symbol of the face difference (zero
+    at k = 0, where E = 1). Adding G to the network's flux makes a macro step propagate the
+    linear part exactly (in particular the fast decay of short-wavelength fluctuations,
+    which matches the noise_filter draw), and, as a flux, it keeps the fixed-point update
+    exactly conservative. FFTs are cuFFT calls through torch.
+    """
+
+    def __init__(self, shape, stencil, model, K: int, device=None, curvature: float | None = None):
+        torch = _torch()
+        st = Stencil(stencil)
+        ny, nx = shape
+        self.shape = (ny, nx)
+        a = 1.0 - st.dt * linear_rate(shape, st, model, curvature)
+        e1 = a ** K - 1.0
+        ty = 2 * np.pi * np.fft.fftfreq(ny)[:, None]
+        tx = 2 * np.pi * np.fft.rfftfreq(nx)[None, :]
+        dxs = (1.0 - np.exp(-1j * tx)) / st.dx
+        dys = (1.0 - np.exp(-1j * ty)) / st.dy
+        den = np.abs(dxs) ** 2 + np.abs(dys) ** 2
+        den[0, 0] = 1.0
+        dtk = K * st.dt
+        mx = -e1 * np.conj(dxs) / den / dtk
+        my = -e1 * np.conj(dys) / den / dtk
+        mx[0, 0] = 0.0
+        my[0, 0] = 0.0
+        dev = device if device is not None else "cuda"
+        self.my = torch.from_numpy(np.broadcast_to(my, (ny, nx // 2 + 1)).astype(np.complex64)).to(dev)
+        self.mx = torch.from_numpy(np.broadcast_to(mx, (ny, nx // 2 + 1)).astype(np.complex64)).to(dev)
+
+    def flux(self, phi):
+        """phi [B, H, W] -> G [B, 2, H, W] (component 0 = y face, 1 = x face)."""
+        torch = _torch()
+        spec = torch.fft.rfft2(phi)
+        gy = torch.fft.irfft2(spec * self.my, s=self.shape)
+        gx = torch.fft.irfft2(spec * self.mx, s=self.shape)
+        return torch.stack([gy, gx], dim=1)
+
+
 class LearnedStepper:
     """Advance one field by K Euler steps per network evaluation, with plain fallback.
 
     Args:
-        net: trained :class:`FluxNet`.
+        net: trained :class:`FluxNet` (captured as it is when the first macro step runs).
         field: initial field (ny, nx), ncols % 128 == 0.
         stencil, model: as for :class:`Integrator` (dx = dy = 1 is what the network saw).
         K: Euler steps per macro step (the K the network was trained for).
         check_every: macro steps per verified span.
         tol: largest accepted relative residual ||learned - plain|| / ||plain - start|| of the
-            checked deterministic macro step.
+            checked deterministic macro step's increments.
+        residual_sigma: if > 0, compare Gaussian low-passed increments (width in sites).
         bound: |phi| above which a state is rejected.
+        use_graph: replay the learned macro step from a CUDA graph (captured on first use).
+        filter_noise: shape the K-step noise draw with :func:`noise_filter` (the K-step
+            accumulation of the linearised plain scheme); without it the K one-step draws
+            are summed undamped, which overstates the high-wavenumber noise.
     """
 
     def __init__(self, net: FluxNet, field, stencil, model, *, K: int = 50, seed: int = 0, check_every: int = 20,
-                 tol: float = 0.5, bound: float = 3.0, plain_precision: str = "f32"):
+                 tol: float = 0.5, bound: float = 3.0, plain_precision: str = "f32", use_graph: bool = True,
+                 filter_noise: bool = True, residual_sigma: float = 0.0):
         torch = _torch()
         self.net = net
         self.stencil = Stencil(stencil)
@@ -413,11 +541,16 @@ class LearnedStepper:
         self.params = model_params_tensor([self.model], dev)
         self.flag = torch.zeros(1, dtype=torch.int32, device=dev)
         self.step_dev = torch.zeros(1, dtype=torch.int64, device=dev)
-        self.xi = torch.empty(2, *self.shape, dtype=torch.float32, device=dev)
+        self.xi = torch.zeros(2, *self.shape, dtype=torch.float32, device=dev)
         self.macro_steps = 0
         self.learned_steps = 0
         self.fallback_spans = 0
         self.residuals = []
+        self._g = noise_filter(self.shape, self.stencil, self.model, self.K).to(dev) if filter_noise else None
+        self._linear = LinearPart(self.shape, self.stencil, self.model, self.K, dev) if net.linear_split else None
+        self._wres = lowpass_weights(self.shape, residual_sigma, dev) if residual_sigma > 0 else None
+        self.use_graph = bool(use_graph)
+        self._graph = None
         quiet = Model(self.model)
         quiet.T = 0.0
         self._plain = Integrator(host, self.stencil, self.model, precision=plain_precision, seed=self.seed ^ 0x5EED)
@@ -436,15 +569,52 @@ class LearnedStepper:
         return int(self.phi_q.to(dtype=_torch().int64).sum().item())
 
     def _flux(self):
-        return self.net.forward(network_input(self.phi_f.unsqueeze(0), self.params))
+        flux = self.net.forward(network_input(self.phi_f.unsqueeze(0), self.params))
+        if self._linear is not None:
+            flux = flux + self._linear.flux(self.phi_f.unsqueeze(0))
+        return flux
 
     def _apply(self, flux, noisy: bool) -> None:
-        T = self.model.T if noisy else 0.0
-        _check(N.lib().amb_learned_update(_ptr(flux), self.shape[0], self.shape[1], self.dtk, self.stencil.dx,
-                                          self.stencil.dy, T, self.seed, _ptr(self.step_dev), _ptr(self.xi),
-                                          _ptr(self.phi_q), _ptr(self.phi_f), self.bound, _ptr(self.flag),
-                                          _stream()))
+        torch = _torch()
+        lib = N.lib()
+        ny, nx = self.shape
+        xi, mag = None, 0.0
+        if noisy and self.model.T > 0:
+            _check(lib.amb_learned_noise(ny, nx, self.seed, _ptr(self.step_dev), _ptr(self.xi), _stream()))
+            if self._g is not None:
+                self.xi.copy_(torch.fft.irfft2(torch.fft.rfft2(self.xi) * self._g, s=(ny, nx)))
+            xi = self.xi
+            mag = math.sqrt(2.0 * self.model.T) * math.sqrt(1.0 / (self.dtk * self.stencil.dx * self.stencil.dy))
+        _check(lib.amb_learned_update(_ptr(flux), ny, nx, self.dtk, self.stencil.dx, self.stencil.dy, _ptr(xi), mag,
+                                      _ptr(self.phi_q), _ptr(self.phi_f), self.bound, _ptr(self.flag), _stream()))
         self.step_dev.add_(1)
+
+    def _macro_step(self) -> None:
+        """One learned macro step (network, noise, fixed-point update, step counter).
+        With use_graph the sequence is captured into a CUDA graph on first use and
+        replayed afterwards (the network's weights are fixed from then on)."""
+        torch = _torch()
+        noisy = self.model.T > 0
+        if self.use_graph and self._graph is None:
+            self.net.refresh()
+            saved = (self.phi_q.clone(), self.step_dev.clone(), self.flag.clone())
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):  # one eager pass first: allocator pools, cuFFT plans
+                self._apply(self._flux(), noisy=noisy)
+            torch.cuda.current_stream().wait_stream(side)
+            self.phi_q.copy_(saved[0])
+            self.phi_f.copy_((self.phi_q.double() / FIX).float())
+            self.step_dev.copy_(saved[1])
+            self.flag.copy_(saved[2])
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):  # records only; the state changes at replay
+                self._apply(self._flux(), noisy=noisy)
+            self._graph = g
+        if self._graph is not None:
+            self._graph.replay()
+        else:
+            self._apply(self._flux(), noisy=noisy)
 
     def _set_from_float(self, f) -> None:
         self.phi_q.copy_(torch_round_fix(f))
@@ -460,8 +630,9 @@ class LearnedStepper:
         self._set_from_float(sim.field_tensor)
 
     def _check_step(self) -> bool:
-        """One deterministic macro step learned vs plain from the current state;
-        returns whether it is within tol (the state is not advanced)."""
+        """One deterministic macro step learned vs plain from the current state; returns
+        whether the relative residual of the increments is within tol (the state is not
+        advanced)."""
         torch = _torch()
         start = self.phi_f.clone()
         sim = self._check_sim
@@ -469,17 +640,18 @@ class LearnedStepper:
         if sim._residual is not None:
             sim._residual.zero_()
         sim.run(self.K)
-        plain = sim.field_tensor.float()
-        pred = start - self.dtk * divergence(self._flux(), self.stencil.dx, self.stencil.dy)[0]
-        num = torch.linalg.vector_norm(pred - plain)
-        den = torch.linalg.vector_norm(plain - start)
+        dplain = sim.field_tensor.float() - start
+        dpred = -self.dtk * divergence(self._flux(), self.stencil.dx, self.stencil.dy)[0]
+        if self._wres is not None:
+            dpred, dplain = lowpass(dpred, self._wres), lowpass(dplain, self._wres)
+        num = torch.linalg.vector_norm(dpred - dplain)
+        den = torch.linalg.vector_norm(dplain)
         res = float((num / torch.clamp(den, min=1e-30)).item())
         self.residuals.append(res)
         return res <= self.tol and math.isfinite(res)
 
     def advance(self, n_macro: int) -> None:
         """Advance n_macro macro steps (each K Euler steps)."""
-        torch = _torch()
         left = int(n_macro)
         while left > 0:
             span = min(self.check_every, left)
@@ -487,10 +659,10 @@ class LearnedStepper:
             snap_step = self.step_dev.clone()
             self.flag.zero_()
             for _ in range(span - 1):
-                self._apply(self._flux(), noisy=self.model.T > 0)
+                self._macro_step()
             ok = self._check_step() and int(self.flag.item()) == 0
             if ok:
-                self._apply(self._flux(), noisy=self.model.T > 0)
+                self._macro_step()
                 ok = int(self.flag.item()) == 0
             if ok:
                 self.learned_steps += span
@@ -504,7 +676,6 @@ class LearnedStepper:
             self.macro_steps += span
             left -= span
         self.net.check_error()
-        del torch
 
     def run_for_time(self, t: float) -> None:
         n = int(round(t / self.dtk))
@@ -517,3 +688,179 @@ def torch_round_fix(f):
     """float field -> int32 fixed point (round to nearest)."""
     torch = _torch()
     return torch.round(f.double() * FIX).to(torch.int32)
+
+
+# ---------------------------------------------------- training and evaluation runs
+
+DEFAULT_SAMPLE_STEPS = (0, 1000, 3000, 10000, 30000, 100000, 200000, 400000, 700000, 1000000)
+
+
+def train_default(out: str | None = None, *, n_traj: int = 512, size: int = 128, K: int = 50, dt: float = 1e-3,
+                  sample_steps=DEFAULT_SAMPLE_STEPS, iters: int = 8000, batch: int = 16, lr: float = 2e-3,
+                  seed: int = 0, holdout: float = 0.1, lowpass_sigma: float = 0.0, highpass_weight: float = 1.0,
+                  log=print) -> tuple[FluxNet, dict]:
+    """Generate pairs with the plain integrator, train a FluxNet on the device kernels,
+    report the held-out error, and optionally save the weights (``FluxNet.load``)."""
+    import time
+    torch = _torch()
+    t0 = time.perf_counter()
+    phi, delta, params, _ = generate_pairs(n_traj, size, K, sample_steps, dt=dt, seed=seed)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    n_test = max(1, int(round(holdout * n_traj)))
+    tr = (phi[:, :-n_test], delta[:, :-n_test], params[:-n_test])
+    te = (phi[:, -n_test:], delta[:, -n_test:], params[-n_test:])
+    net = FluxNet(seed=seed)
+    # the linear part depends on (a, c, kappa, dt, shape) only, which the pair set shares
+    lin = LinearPart((size, size), Stencil(dt, 1, 1), Model(a=-0.25, b=0, c=0.25, kappa=1), K)
+    zero = FluxNet(seed=seed)
+    for w in zero.weights:
+        w.zero_()
+    linear_only = evaluate(zero, *te, K=K, dt=dt, linear=lin)
+    before = evaluate(net, *te, K=K, dt=dt, linear=lin)
+    t1 = time.perf_counter()
+    hist = train(net, *tr, K=K, dt=dt, iters=iters, batch=batch, lr=lr, seed=seed, log_every=max(1, iters // 20),
+                 lowpass_sigma=lowpass_sigma, highpass_weight=highpass_weight, linear=lin)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t1
+    after = evaluate(net, *te, K=K, dt=dt, linear=lin)
+    after_lp = evaluate(net, *te, K=K, dt=dt, lowpass_sigma=2.0, linear=lin)
+    info = {"n_traj": n_traj, "size": size, "K": K, "dt": dt, "sample_steps": list(sample_steps), "iters": iters,
+            "batch": batch, "lr": lr, "seed": seed, "pairs": int(phi.shape[0] * phi.shape[1]),
+            "data_seconds": t_data, "train_seconds": t_train, "heldout_rel_mse_linear_part_only": linear_only,
+            "heldout_rel_mse_untrained": before,
+            "heldout_rel_mse": after, "heldout_rel_mse_lowpass2": after_lp, "lowpass_sigma": lowpass_sigma,
+            "highpass_weight": highpass_weight, "loss_history": hist}
+    if log:
+        log(f"data {t_data:.1f} s, train {t_train:.1f} s, held-out relative MSE: linear part alone "
+            f"{linear_only:.3g}, untrained {before:.3g}, trained {after:.3g} (low-passed {after_lp:.3g})")
+    if out:
+        net.save(out, K=K, dt=dt, heldout_rel_mse=after, heldout_rel_mse_lowpass2=after_lp, iters=iters,
+                 n_traj=n_traj, size=size, lowpass_sigma=lowpass_sigma)
+    del phi, delta
+    return net, info
+
+
+def _timed(fn):
+    import time
+    torch = _torch()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fn()
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0
+
+
+def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: int = 50, seed: int = 0,
+                       check_every: int = 20, tol: float = 0.5, plain_seeds=(1, 2, 3), residual_sigma: float = 2.0,
+                       filter_noise: bool = True) -> dict:
+    """Time to ``t_end`` and end-state statistics of the learned stepper against the plain
+    FP32 integrator (the faster of the Integrator and a one-replica CUDA-graph ensemble)
+    from the same initial field: S(k) mean wavenumber (the reference notebook's
+    definition), droplet count, mass. The plain run is repeated with ``plain_seeds`` to
+    show the spread of its statistics."""
+    from .analysis import count_droplets, mean_wavenumber, structure_factor
+    stencil, model = Stencil(stencil), Model(model)
+    nsteps = int(round(t_end / stencil.dt))
+    field = np.asarray(field, dtype=np.float64)
+    phi0 = float(field.mean())
+    res = {"t_end": t_end, "K": K, "shape": list(field.shape), "model": model.as_dict(), "tol": tol,
+           "check_every": check_every, "residual_sigma": residual_sigma, "filter_noise": filter_noise, "plain": []}
+    probe = max(1, min(nsteps, 20000))
+    sim = Integrator(field, stencil, model, precision="f32", seed=0)
+    t_int = _timed(lambda: sim.run(probe))
+    res["plain_kernel_config"] = getattr(sim, "kernel_config", None)
+    del sim
+    ens = Ensemble([field], stencil, model, precision="f32", seeds=[0], graph_steps=50)
+    t_ens = _timed(lambda: ens.run(probe))
+    ens.close()
+    use_ensemble = t_ens < t_int
+    res["plain_path"] = "ensemble" if use_ensemble else "integrator"
+    res["plain_probe_us_per_step"] = {"integrator": 1e6 * t_int / probe, "ensemble": 1e6 * t_ens / probe}
+    for sd in plain_seeds:
+        if use_ensemble:
+            ens = Ensemble([field], stencil, model, precision="f32", seeds=[sd], graph_steps=50)
+            sec = _timed(lambda: ens.run(nsteps))
+            f = ens.field(0)
+            ens.close()
+        else:
+            sim = Integrator(field, stencil, model, precision="f32", seed=sd)
+            sec = _timed(lambda: sim.run(nsteps))
+            f = sim.field
+            del sim
+        k, S, _ = structure_factor(f, stencil.dx, stencil.dy, phi0=phi0)
+        res["plain"].append({"seconds": sec, "seed": sd, "k_avg": mean_wavenumber(k, S),
+                             "k_peak": float(k[np.nanargmax(S)]), "droplets": count_droplets(f, phi0),
+                             "mass_drift": float(f.sum() - field.sum())})
+    st = LearnedStepper(net, field, stencil, model, K=K, seed=seed, check_every=check_every, tol=tol,
+                        residual_sigma=residual_sigma, filter_noise=filter_noise)
+    m0 = st.mass_q()
+    sec = _timed(lambda: st.run_for_time(t_end))
+    f = st.field
+    k, S, _ = structure_factor(f, stencil.dx, stencil.dy, phi0=phi0)
+    res["learned"] = {"seconds": sec, "k_avg": mean_wavenumber(k, S), "k_peak": float(k[np.nanargmax(S)]),
+                      "droplets": count_droplets(f, phi0), "mass_q_drift": st.mass_q() - m0,
+                      "macro_steps": st.macro_steps, "learned_macro_steps": st.learned_steps,
+                      "fallback_spans": st.fallback_spans,
+                      "median_residual": float(np.median(st.residuals)) if st.residuals else None}
+    plain_k = np.array([p["k_avg"] for p in res["plain"]])
+    res["plain_k_avg_mean"] = float(plain_k.mean())
+    res["plain_k_avg_std"] = float(plain_k.std())
+    res["k_avg_rel_err"] = abs(res["learned"]["k_avg"] - plain_k.mean()) / plain_k.mean()
+    res["plain_seconds_min"] = float(min(p["seconds"] for p in res["plain"]))
+    res["speedup"] = res["plain_seconds_min"] / sec
+    return res
+
+
+def _main(argv=None) -> int:
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(prog="python -m activemodelbplus.learned")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    t = sub.add_parser("train", help="generate pairs with the plain integrator and train the flux network")
+    t.add_argument("--out", required=True)
+    t.add_argument("--n-traj", type=int, default=512)
+    t.add_argument("--size", type=int, default=128)
+    t.add_argument("--iters", type=int, default=8000)
+    t.add_argument("--batch", type=int, default=16)
+    t.add_argument("--lr", type=float, default=2e-3)
+    t.add_argument("--seed", type=int, default=0)
+    t.add_argument("--info", default=None, help="write the run summary (JSON) here")
+    t.add_argument("--sample-steps", default=",".join(str(v) for v in DEFAULT_SAMPLE_STEPS))
+    t.add_argument("--lowpass-sigma", type=float, default=0.0)
+    t.add_argument("--highpass-weight", type=float, default=1.0)
+    c = sub.add_parser("compare", help="time to t_end, learned vs plain FP32, from one seeded field")
+    c.add_argument("--weights", required=True)
+    c.add_argument("--size", type=int, default=512)
+    c.add_argument("--t-end", type=float, default=1000.0)
+    c.add_argument("--check-every", type=int, default=20)
+    c.add_argument("--tol", type=float, default=0.5)
+    c.add_argument("--seed", type=int, default=0)
+    c.add_argument("--temperature", type=float, default=0.05)
+    c.add_argument("--residual-sigma", type=float, default=2.0)
+    c.add_argument("--no-noise-filter", action="store_true")
+    c.add_argument("--plain-seeds", default="1,2,3")
+    a = ap.parse_args(argv)
+    if a.cmd == "train":
+        steps = [int(v) for v in a.sample_steps.split(",")]
+        _, info = train_default(a.out, n_traj=a.n_traj, size=a.size, iters=a.iters, batch=a.batch, lr=a.lr,
+                                seed=a.seed, sample_steps=steps, lowpass_sigma=a.lowpass_sigma,
+                                highpass_weight=a.highpass_weight)
+        if a.info:
+            with open(a.info, "w") as fh:
+                json.dump(info, fh, indent=1)
+        return 0
+    net = FluxNet.load(a.weights)
+    rng = np.random.default_rng(a.seed)
+    field = -0.4 + 0.01 * rng.standard_normal((a.size, a.size))
+    model = Model(a=-0.25, b=0, c=0.25, kappa=1, lamb=-1, zeta=-4, T=a.temperature)
+    res = compare_with_plain(net, field, Stencil(1e-3, 1, 1), model, t_end=a.t_end, seed=a.seed,
+                             check_every=a.check_every, tol=a.tol, residual_sigma=a.residual_sigma,
+                             filter_noise=not a.no_noise_filter,
+                             plain_seeds=tuple(int(v) for v in a.plain_seeds.split(",")))
+    print(json.dumps(res))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(_main())

@@ -124,6 +124,12 @@ extern "C" int amb_step_f32_ex(const amb_stencil* stencil, const amb_model* mode
     if (nsteps < 0) return fail(AMB_ERR_INVALID, "nsteps must be >= 0");
     amb_kernel_config cfg{AMB_KERNEL_AUTO, 0, 0, 0};
     if (config) cfg = *config;
+    if (cfg.kernel == AMB_KERNEL_AUTO && cfg.seg_rows == 0 && cfg.pairs_per_cta == 0)
+    {
+        amb_kernel_config tuned;
+        if (amb::autotune_lookup(nrows, ncols, residual != nullptr, model->temperature > 0 && !injected_noise, &tuned))
+            cfg = tuned;  // a sliding choice still falls back to the tile kernel on unaligned buffers below
+    }
     if (cfg.kernel < AMB_KERNEL_AUTO || cfg.kernel > AMB_KERNEL_SLIDING) return fail(AMB_ERR_INVALID, "unknown kernel selector");
     if (cfg.seg_rows < 0 || cfg.pairs_per_cta < 0 || cfg.pairs_per_cta > 4 || cfg.pairs_per_cta == 3)
         return fail(AMB_ERR_INVALID, "kernel config: seg_rows >= 0, pairs_per_cta in {0, 1, 2, 4}");
@@ -134,6 +140,8 @@ extern "C" int amb_step_f32_ex(const amb_stencil* stencil, const amb_model* mode
     const bool fits = amb::step_f32_sliding_supported(nrows, ncols, 0) && aligned(field, 16) && aligned(spare, 16)
                       && (!residual || aligned(residual, 8)) && (!injected_noise || aligned(injected_noise, 16));
     bool sliding = false;
+    if (cfg.kernel == AMB_KERNEL_SLIDING && !fits && !(config && config->kernel == AMB_KERNEL_SLIDING))
+        cfg = amb_kernel_config{AMB_KERNEL_TILE, 0, 0, 0};
     if (cfg.kernel == AMB_KERNEL_SLIDING)
     {
         if (!fits)

@@ -1,0 +1,160 @@
+// Measured choice of the FP32 step kernel and its launch shape for one grid shape
+// (no reference counterpart; the reference launches fixed 8 x 8 blocks).
+//
+// Candidates: the tile kernel, and the warp-pair sliding kernel with 1, 2 or 4
+// pairs per CTA and row-segment heights from 2 rows up to the whole grid (plus the
+// occupancy model's own choice). Each is timed with CUDA events over a few steps on
+// scratch buffers of the same shape; the fastest few are timed again and the best
+// is kept in a process-wide cache keyed by (device, nrows, ncols, compensated,
+// noise), which AMB_KERNEL_AUTO consults. The kernels do the same work whatever the
+// field values, so zero-filled scratch fields time the real workload.
+#include "amb_gb300.h"
+#include "amb_kernels.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+namespace
+{
+    using Key = std::tuple<int, int, int, int, int>;  // device, nrows, ncols, compensated, noise
+    struct Entry
+    {
+        amb_kernel_config config;
+        double us_per_step;
+    };
+    std::map<Key, Entry> g_cache;
+    std::mutex g_mutex;
+
+    struct Scratch
+    {
+        float* a = nullptr;
+        float* b = nullptr;
+        uint16_t* r = nullptr;
+        ~Scratch()
+        {
+            if (a) cudaFree(a);
+            if (b) cudaFree(b);
+            if (r) cudaFree(r);
+        }
+    };
+
+    int key_device()
+    {
+        int d = 0;
+        cudaGetDevice(&d);
+        return d;
+    }
+}
+
+namespace amb
+{
+    bool autotune_lookup(int nrows, int ncols, int compensated, int noise, amb_kernel_config* out)
+    {
+        std::lock_guard<std::mutex> lock(g_mutex);
+        auto it = g_cache.find(Key{key_device(), nrows, ncols, compensated ? 1 : 0, noise ? 1 : 0});
+        if (it == g_cache.end()) return false;
+        *out = it->second.config;
+        return true;
+    }
+}
+
+extern "C" int amb_autotune_f32(const amb_stencil* stencil, const amb_model* model, int nrows, int ncols,
+                                int compensated, int probe_steps, void* stream, amb_kernel_config* best,
+                                double* us_per_step)
+{
+    if (!stencil || !model || !best || nrows < 1 || ncols < 1 || probe_steps < 1 || probe_steps > 1000)
+    {
+        amb::set_last_error("amb_autotune_f32: bad arguments (probe_steps in [1, 1000])");
+        return AMB_ERR_INVALID;
+    }
+    const int noise = model->temperature > 0 ? 1 : 0;
+    const Key key{key_device(), nrows, ncols, compensated ? 1 : 0, noise};
+    {
+        std::lock_guard<std::mutex> lock(g_mutex);
+        auto it = g_cache.find(key);
+        if (it != g_cache.end())
+        {
+            *best = it->second.config;
+            if (us_per_step) *us_per_step = it->second.us_per_step;
+            return AMB_OK;
+        }
+    }
+    const size_t n = size_t(nrows) * ncols;
+    Scratch s;
+    cudaError_t e = cudaMalloc(&s.a, n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&s.b, n * sizeof(float));
+    if (e == cudaSuccess && compensated) e = cudaMalloc(&s.r, n * sizeof(uint16_t));
+    if (e == cudaSuccess) e = cudaMemset(s.a, 0, n * sizeof(float));
+    if (e == cudaSuccess && compensated) e = cudaMemset(s.r, 0, n * sizeof(uint16_t));
+    if (e != cudaSuccess)
+    {
+        amb::set_last_error(std::string("amb_autotune_f32: ") + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? AMB_ERR_NOMEM : AMB_ERR_CUDA;
+    }
+
+    std::vector<amb_kernel_config> cands;
+    cands.push_back({AMB_KERNEL_TILE, 0, 0, 0});
+    if (ncols >= 112 && ncols % 4 == 0)
+        for (int pairs : {1, 2, 4})
+        {
+            cands.push_back({AMB_KERNEL_SLIDING, 0, pairs, 0});
+            for (int seg = 2; seg < 2 * nrows && seg <= 4096; seg *= 2)
+                cands.push_back({AMB_KERNEL_SLIDING, std::min(seg, nrows), pairs, 0});
+        }
+
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    auto time_one = [&](const amb_kernel_config& c, float* ms) -> int {
+        int in_spare = 0;
+        int rc = amb_step_f32_ex(stencil, model, 1, nrows, ncols, s.a, s.b, s.r, 0, 2, nullptr, &c, stream, &in_spare);
+        if (rc) return rc;
+        cudaEventRecord(t0, static_cast<cudaStream_t>(stream));
+        rc = amb_step_f32_ex(stencil, model, 1, nrows, ncols, s.a, s.b, s.r, 2, probe_steps, nullptr, &c, stream,
+                             &in_spare);
+        if (rc) return rc;
+        cudaEventRecord(t1, static_cast<cudaStream_t>(stream));
+        if (cudaEventSynchronize(t1) != cudaSuccess) return AMB_ERR_CUDA;
+        cudaEventElapsedTime(ms, t0, t1);
+        return AMB_OK;
+    };
+
+    std::vector<std::pair<float, int>> times;
+    int rc = AMB_OK;
+    for (size_t i = 0; i < cands.size() && rc == AMB_OK; ++i)
+    {
+        float ms = 0.f;
+        rc = time_one(cands[i], &ms);
+        if (rc == AMB_OK) times.push_back({ms, int(i)});
+    }
+    if (rc == AMB_OK)
+    {
+        std::sort(times.begin(), times.end());
+        // second round for the leaders: keep each one's faster time
+        const size_t lead = std::min<size_t>(4, times.size());
+        for (size_t j = 0; j < lead && rc == AMB_OK; ++j)
+        {
+            float ms = 0.f;
+            rc = time_one(cands[times[j].second], &ms);
+            if (rc == AMB_OK) times[j].first = std::min(times[j].first, ms);
+        }
+        std::sort(times.begin(), times.begin() + lead);
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if (rc != AMB_OK) return rc;
+    *best = cands[times[0].second];
+    const double us = 1000.0 * times[0].first / probe_steps;
+    if (us_per_step) *us_per_step = us;
+    {
+        std::lock_guard<std::mutex> lock(g_mutex);
+        g_cache[key] = Entry{*best, us};
+    }
+    return AMB_OK;
+}

@@ -960,23 +960,32 @@ extern "C" int amb_learned_input(const float* phi, const float* params, int batc
     return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_input", e);
 }
 
+extern "C" int amb_learned_noise(int nrows, int ncols, uint64_t seed, const int64_t* step, float* xi, void* stream)
+{
+    if (!step || !xi || nrows < 1 || ncols < 1) return fail_invalid("amb_learned_noise: bad arguments");
+    const size_t n = size_t(nrows) * ncols;
+    const int grid = int(std::min<size_t>((n + 255) / 256, size_t(sm_count()) * 16));
+    learned_noise_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(xi, nrows, ncols, seed, step);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_noise", e);
+}
+
 extern "C" int amb_learned_update(const float* flux, int nrows, int ncols, double dt_macro, double dx, double dy,
-                                  double temperature, uint64_t seed, const int64_t* step, float* xi_scratch,
-                                  int32_t* phi_q, float* phi_f, double bound, int* flag, void* stream)
+                                  const float* xi, double noise_mag, int32_t* phi_q, float* phi_f, double bound,
+                                  int* flag, void* stream)
 {
     if (!flux || !phi_q || !phi_f || !flag || nrows < 1 || ncols < 1 || !(dt_macro > 0) || !(dx > 0) ||
-        !(dy > 0) || temperature < 0 || !(bound > 0) || (temperature > 0 && (!step || !xi_scratch)))
+        !(dy > 0) || !(noise_mag >= 0) || !(bound > 0))
         return fail_invalid("amb_learned_update: bad arguments");
     auto s = static_cast<cudaStream_t>(stream);
     const size_t n = size_t(nrows) * ncols;
     const int grid = int(std::min<size_t>((n + 255) / 256, size_t(sm_count()) * 16));
-    const bool noisy = temperature > 0;
-    if (noisy) learned_noise_kernel<<<grid, 256, 0, s>>>(xi_scratch, nrows, ncols, seed, step);
     const double fix = 16777216.0;
-    const double noise_mag = noisy ? std::sqrt(2.0 * temperature) * std::sqrt(1.0 / (dt_macro * dx * dy)) : 0.0;
     const double qb = std::min(bound * fix, 2.0e9);
-    learned_update_kernel<<<grid, 256, 0, s>>>(flux, noisy ? xi_scratch : nullptr, nrows, ncols, dt_macro / dy * fix,
-                                               dt_macro / dx * fix, noise_mag, phi_q, phi_f, (long long)qb, flag);
+    const bool noisy = xi && noise_mag > 0;
+    learned_update_kernel<<<grid, 256, 0, s>>>(flux, noisy ? xi : nullptr, nrows, ncols, dt_macro / dy * fix,
+                                               dt_macro / dx * fix, noisy ? noise_mag : 0.0, phi_q, phi_f,
+                                               (long long)qb, flag);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_update", e);
 }

@@ -3,6 +3,7 @@
 #pragma once
 
 #include "amb_common.cuh"
+#include "amb_gb300.h"
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -54,6 +55,9 @@ namespace amb
 
     template <typename Real>
     cudaError_t launch_nonfinite(const Real* f, size_t n, int* flag, cudaStream_t stream);
+
+    // Tuned FP32 step configuration for this shape (amb_autotune_f32's cache), if any.
+    bool autotune_lookup(int nrows, int ncols, int compensated, int noise, amb_kernel_config* out);
 
     // Sets the message amb_last_error() returns on the calling thread.
     void set_last_error(const std::string& msg);

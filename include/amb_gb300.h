@@ -154,6 +154,17 @@ int amb_step_f32(const amb_stencil* stencil, const amb_model* model, uint64_t se
                  float* field, float* spare, uint16_t* residual, int64_t step0, int nsteps,
                  const float* injected_noise, int kernel, void* stream, int* result_in_spare);
 
+/* Measured kernel choice (no reference counterpart): times the tile kernel and the sliding
+ * kernel over a range of row-segment heights and warp pairs per CTA, a few steps each on
+ * scratch buffers of this shape (zero field, this model's noise on or off), and returns the
+ * fastest configuration and its time per step. The result is cached per (device, shape,
+ * compensated, noise); later calls return the cached entry, and AMB_KERNEL_AUTO in
+ * amb_step_f32 / amb_step_f32_ex uses it. Synchronous; allocates 2-3 fields of scratch. The
+ * two FP32 kernels agree to FP32 rounding, not bitwise: request a kernel explicitly for
+ * results that must not depend on a timing. */
+int amb_autotune_f32(const amb_stencil* stencil, const amb_model* model, int nrows, int ncols, int compensated,
+                     int probe_steps, void* stream, amb_kernel_config* best, double* us_per_step);
+
 /* amb_step_f32 with an explicit kernel configuration (NULL = defaults). */
 int amb_step_f32_ex(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows, int ncols,
                     float* field, float* spare, uint16_t* residual, int64_t step0, int nsteps,
@@ -274,18 +285,23 @@ int amb_conv5x5_wgrad(const void* x, const void* dz, int batch, int nrows, int n
  * lambda, 10*T, zeros. phi: [batch][nrows][ncols] FP32; params: [batch][3] = (zeta, lambda, T). */
 int amb_learned_input(const float* phi, const float* params, int batch, int nrows, int ncols, void* x, void* stream);
 
+/* Two standard normals per site, xi[2][nrows][ncols], Philox keyed (seed, *step, site,
+ * component) exactly as the integrator's noise (the step is read from device memory so that
+ * a captured graph can advance it). */
+int amb_learned_noise(int nrows, int ncols, uint64_t seed, const int64_t* step, float* xi, void* stream);
+
 /* One macro step of the learned stepper on a fixed-point field phi_q (int32, phi * 2^24):
  * phi -= dt_macro * div F, F = flux + noise flux, with div the face difference
  * (F_x(r,c) - F_x(r,c-1))/dx + (F_y(r,c) - F_y(r-1,c))/dy. flux: [2][nrows][ncols] FP32
- * (component 0 = y face after (r,c), 1 = x face). For temperature > 0 the noise flux is the
- * order-8 central derivative of sqrt(2T/(dt_macro dx dy)) xi written as face sums, xi
- * Philox normals keyed (seed, *step, site) (xi_scratch: 2*nrows*ncols floats). Every face
- * increment is rounded to an integer once and applied with opposite signs to its two sites,
- * so sum(phi_q) is conserved exactly. phi_f receives phi_q * 2^-24. *flag |= 1 if the flux is
- * non-finite or |phi| exceeds bound (then clamped). */
+ * (component 0 = y face after (r,c), 1 = x face). If xi is non-NULL the noise flux is the
+ * order-8 central derivative of noise_mag * xi written as face sums (xi as from
+ * amb_learned_noise, possibly filtered by the caller). Every face increment is rounded to an
+ * integer once and applied with opposite signs to its two sites, so sum(phi_q) is conserved
+ * exactly. phi_f receives phi_q * 2^-24. *flag |= 1 if the flux is non-finite or |phi|
+ * exceeds bound (then clamped). */
 int amb_learned_update(const float* flux, int nrows, int ncols, double dt_macro, double dx, double dy,
-                       double temperature, uint64_t seed, const int64_t* step, float* xi_scratch, int32_t* phi_q,
-                       float* phi_f, double bound, int* flag, void* stream);
+                       const float* xi, double noise_mag, int32_t* phi_q, float* phi_f, double bound, int* flag,
+                       void* stream);
 
 #ifdef __cplusplus
 }

@@ -129,3 +129,27 @@ def test_sliding_rejects_unsupported_shapes():
     rc = N.lib().amb_step_f32_ex(ctypes.byref(s), ctypes.byref(m), 0, 32, 100, a.data_ptr(), b.data_ptr(), None, 0, 1,
                                  None, ctypes.byref(cfg), torch.cuda.current_stream().cuda_stream, None)
     assert rc == 0
+
+
+def test_autotuner_choice_is_used_and_cached():
+    """amb_autotune_f32 returns a valid configuration, caches it, and AMB_KERNEL_AUTO then
+    runs exactly that configuration (bitwise equal to requesting it explicitly)."""
+    import torch
+    N = native()
+    p = Params(T=0.05, **AMB)
+    s = N.amb_stencil(p.dt, p.dx, p.dy)
+    m = N.amb_model(p.a, p.b, p.c, p.kappa, p.lamb, p.zeta, p.T)
+    cfg, us = N.amb_kernel_config(), ctypes.c_double()
+    strm = torch.cuda.current_stream().cuda_stream
+    assert N.lib().amb_autotune_f32(ctypes.byref(s), ctypes.byref(m), 96, 448, 1, 4, strm, ctypes.byref(cfg),
+                                    ctypes.byref(us)) == 0, N.last_error()
+    assert cfg.kernel in (N.AMB_KERNEL_TILE, N.AMB_KERNEL_SLIDING) and us.value > 0
+    cfg2, us2 = N.amb_kernel_config(), ctypes.c_double()
+    assert N.lib().amb_autotune_f32(ctypes.byref(s), ctypes.byref(m), 96, 448, 1, 4, strm, ctypes.byref(cfg2),
+                                    ctypes.byref(us2)) == 0
+    assert (cfg2.kernel, cfg2.seg_rows, cfg2.pairs_per_cta, us2.value) == (cfg.kernel, cfg.seg_rows,
+                                                                           cfg.pairs_per_cta, us.value)
+    field = initial((96, 448), seed=12)
+    auto = run_f32(field, p, 10, kernel=0)
+    explicit = run_f32(field, p, 10, kernel=cfg.kernel, seg_rows=cfg.seg_rows, pairs=cfg.pairs_per_cta)
+    assert np.array_equal(auto, explicit)

@@ -95,6 +95,20 @@ def test_conv_forward_f32(shape, cin_used, cin, cout, npad):
     assert np.abs(got - ref).max() < 2e-5 * max(1.0, np.abs(ref).max())
 
 
+@pytest.mark.parametrize("shape", [(4, 64, 512), (16, 128, 128), (1, 512, 512), (3, 45, 256)])
+def test_conv_forward_multirow_ctas(shape):
+    """Shapes where each CTA stages many rows (up to 16) across several 128-site windows,
+    as in inference on 512 x 512 fields and training on batches of 128 x 128 fields."""
+    B, H, W = shape
+    rng = np.random.default_rng(B * H + W)
+    x = OL.bf16_round(rng.standard_normal((B, 32, H, W)))
+    w = OL.bf16_round(rng.standard_normal((32, 32, 5, 5)) * 0.05)
+    b = rng.standard_normal(32).astype(np.float32)
+    got, _ = run_conv(x, w, b, cin=32, npad=32, cout=32, epilogue=1)
+    ref = OL.conv5x5(x, w, b.astype(np.float64))
+    assert np.abs(got - ref).max() < 2e-5 * max(1.0, np.abs(ref).max())
+
+
 @pytest.mark.parametrize("shape", SHAPES[:3])
 def test_conv_forward_gelu(shape):
     B, H, W = shape
@@ -211,13 +225,15 @@ def test_update_is_exact_and_conservative(T):
     flag = torch.zeros(1, dtype=torch.int32, device="cuda")
     dtk = 0.05
     flux_dev = torch.from_numpy(flux).cuda()
-    rc = N.lib().amb_learned_update(flux_dev.data_ptr(), H, W, dtk, 1.0, 1.0, T, 99,
-                                    step.data_ptr(), xi.data_ptr(), q.data_ptr(), f.data_ptr(), 3.0,
-                                    flag.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    lib, strm = N.lib(), torch.cuda.current_stream().cuda_stream
+    mag = math.sqrt(2 * T) * math.sqrt(1 / (dtk * 1.0 * 1.0))
+    if T > 0:
+        assert lib.amb_learned_noise(H, W, 99, step.data_ptr(), xi.data_ptr(), strm) == 0, N.last_error()
+    rc = lib.amb_learned_update(flux_dev.data_ptr(), H, W, dtk, 1.0, 1.0, xi.data_ptr() if T > 0 else None, mag,
+                                q.data_ptr(), f.data_ptr(), 3.0, flag.data_ptr(), strm)
     assert rc == 0, N.last_error()
     got = q.cpu().numpy().astype(np.int64)
     if T > 0:
-        mag = math.sqrt(2 * T) * math.sqrt(1 / (dtk * 1.0 * 1.0))
         ref = OL.face_update(phi_q, flux, dtk, xi=xi.cpu().numpy(), noise_mag=mag)
         import oracle
         xy, xx = oracle.normals(H, W, 99, 7)  # the same Philox-keyed normals, evaluated in double
@@ -286,3 +302,64 @@ def test_training_gains_over_untrained_and_naive_coarse_step():
     naive = num / den
     assert after < 0.5 * before, (before, after)
     assert after < naive, (after, naive)
+
+
+def test_filtered_macro_noise_matches_k_plain_steps():
+    """At a uniform bulk state (phi = 1, where the deterministic flux vanishes) and small T,
+    the noise of one filtered macro step has the same radially binned power spectrum as K
+    plain steps (within 12% per bin over 8 seeds), while the unfiltered draw overstates the
+    high-wavenumber power several-fold."""
+    torch, L, N = mods()
+    from activemodelbplus.integrator import Integrator, Model, Stencil
+    H = W = 128
+    K = 50
+    st = Stencil(1e-3, 1, 1)
+    m = Model(-0.25, 0, 0.25, 1, 0, 0, 1e-4)
+    net = L.FluxNet(seed=0)
+    net.weights[-1].zero_()
+    net.biases[-1].zero_()
+    kk = np.hypot(*np.meshgrid(np.fft.fftfreq(H), np.fft.fftfreq(W), indexing="ij")).ravel()
+    bins = np.digitize(kk, np.linspace(0, 0.71, 15))
+
+    def spectrum(d):
+        p = np.abs(np.fft.fft2(d)).ravel() ** 2
+        return np.array([p[bins == b].mean() for b in range(1, 15)])
+
+    sp_plain, sp_f, sp_u = 0, 0, 0
+    for seed in range(8):
+        sim = Integrator(np.ones((H, W)), st, m, precision="f64", seed=100 + seed)
+        sim.run(K)
+        sp_plain = sp_plain + spectrum(sim.field - 1.0)
+        for filt in (True, False):
+            s = L.LearnedStepper(net, np.ones((H, W)), st, m, K=K, seed=200 + seed, check_every=1, tol=1e9,
+                                 filter_noise=filt, use_graph=False)
+            s.advance(1)
+            d = s.field - 1.0
+            if filt:
+                sp_f = sp_f + spectrum(d)
+            else:
+                sp_u = sp_u + spectrum(d)
+    ratio = sp_f / sp_plain
+    assert np.all(np.abs(ratio - 1) < 0.12), ratio
+    assert (sp_u / sp_plain).max() > 3, sp_u / sp_plain
+
+
+def test_stepper_graph_replay_equals_eager():
+    """The CUDA-graph replay of a learned macro step (with filtered noise) gives bitwise the
+    state of the eager path."""
+    torch, L, N = mods()
+    from activemodelbplus.integrator import Model, Stencil
+    field = -0.4 + 0.05 * np.random.default_rng(9).standard_normal((64, 256))
+    net = L.FluxNet(seed=5)
+    for w in net.weights:
+        w.mul_(0.1)
+    net.refresh()
+    m = Model(-0.25, 0, 0.25, 1, -1, -4, 0.05)
+    out = []
+    for graph in (True, False):
+        s = L.LearnedStepper(net, field, Stencil(1e-3, 1, 1), m, K=50, seed=3, check_every=6, tol=1e9,
+                             use_graph=graph)
+        s.advance(12)
+        assert s.learned_steps == 12
+        out.append(s.phi_q.cpu().numpy())
+    assert np.array_equal(out[0], out[1])

@@ -154,3 +154,35 @@ def test_network_oracle_gradients_match_finite_differences():
     fd = ((OL.fluxnet(x, ws, bp, bf16_activations=False) - OL.fluxnet(x, ws, bm, bf16_activations=False))
           * dflux).sum() / (2 * eps)
     assert abs(fd - gb[0][1]) < 1e-6
+
+
+@pytest.mark.parametrize("mode", [(0, 3), (5, 0), (7, 11), (31, 31), (20, 64)])
+def test_linear_rate_matches_one_oracle_step(mode):
+    """A small mode about the bulk state phi = 1 decays in one step of the reference scheme
+    (the CPU oracle, lambda = zeta = T = 0) by exactly 1 - dt w(k) to first order."""
+    import oracle
+    from activemodelbplus.integrator import Model, Stencil
+    H, W = 64, 128
+    ky, kx = mode
+    eps = 1e-6
+    r, c = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    pert = np.cos(2 * np.pi * (ky * r / H + kx * c / W))
+    p = oracle.Params(dt=1e-3, dx=1.0, dy=1.0, a=-0.25, b=0.0, c=0.25, kappa=1.0, lamb=0.0, zeta=0.0, T=0.0)
+    after = oracle.run(1.0 + eps * pert, p, 1)
+    ratio = ((after - 1.0) * pert).sum() / (eps * (pert * pert).sum())
+    w = L.linear_rate((H, W), Stencil(1e-3, 1, 1), Model(-0.25, 0, 0.25, 1, 0, 0, 0))
+    assert abs(ratio - (1 - 1e-3 * w[ky, kx])) < 1e-6
+
+
+def test_linear_part_flux_reproduces_the_k_step_propagator():
+    from activemodelbplus.integrator import Model, Stencil
+    H, W, K = 32, 48, 50
+    st, m = Stencil(1e-3, 1, 1), Model(-0.25, 0, 0.25, 1, 0, 0, 0)
+    lin = L.LinearPart((H, W), st, m, K, device="cpu")
+    phi = torch.from_numpy(np.random.default_rng(3).standard_normal((2, H, W))).float()
+    g = lin.flux(phi)
+    new = phi - K * st.dt * L.divergence(g, 1.0, 1.0)
+    a = torch.from_numpy((1 - st.dt * L.linear_rate((H, W), st, m)) ** K).float()
+    ref = torch.fft.irfft2(torch.fft.rfft2(phi) * a, s=(H, W))
+    assert float((new - ref).abs().max()) < 1e-5
+    assert abs(float(new.sum() - phi.sum())) < 1e-3
