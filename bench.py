@@ -62,6 +62,10 @@ def parse_args():
     ap.add_argument("--temperature", type=float, default=0.05)
     ap.add_argument("--ensemble", action="store_true",
                     help="measure the batched ensemble workload (256 replicas of uneven sizes) instead")
+    ap.add_argument("--learned", action="store_true",
+                    help="learned coarse stepper vs plain FP32: time to --t-end on a 512^2 AMB+ field")
+    ap.add_argument("--t-end", type=float, default=1000.0)
+    ap.add_argument("--weights", default=os.path.join(PKG, "activemodelbplus", "weights", "fluxnet_k50.npz"))
     ap.add_argument("--launches", type=int, default=0,
                     help="profiling driver: run this many bare step launches through the C ABI and exit")
     return ap.parse_args()
@@ -433,6 +437,34 @@ def run_ensemble(args):
     ens.close()
 
 
+def run_learned(args):
+    """Learned coarse stepper (K = 50 Euler steps per network evaluation) against the plain
+    FP32 integrator, both from the same seeded 512^2 field (phi = -0.4 + 0.01 N(0,1), numpy seed
+    0; a=-0.25 b=0 c=0.25 kappa=1 lambda=-1 zeta=-4 T=0.05, dt=1e-3) to t_end: wall time of each
+    (CUDA-synchronised), the S(k) mean wavenumber of the end states (the plain one over three
+    noise seeds), droplet counts and the learned run's exact fixed-point mass drift."""
+    import torch
+    from activemodelbplus import learned as L
+    from activemodelbplus.integrator import Model, Stencil
+    net = L.FluxNet.load(args.weights)
+    field = -0.4 + 0.01 * np.random.default_rng(0).standard_normal((512, 512))
+    model = Model(a=-0.25, b=0, c=0.25, kappa=1, lamb=-1, zeta=-4, T=0.05)
+    with ClockSampler(torch.cuda.current_device()) as clocks:
+        res = L.compare_with_plain(net, field, Stencil(1e-3, 1, 1), model, t_end=args.t_end, residual_sigma=2.0)
+    out = {"metric": f"learned vs plain FP32 time to t={args.t_end:g} (512^2 AMB+), speed-up", "value": res["speedup"],
+           "unit": "x", "higher_is_better": True, "n_gpus": 1, "dtype": "bf16 network / int32 fixed-point field",
+           "data": "synthetic", "config": {"workload": "learned_time_to_t", "size": 512, "K": 50,
+                                           "t_end": args.t_end, "check_every": res["check_every"], "tol": res["tol"]},
+           "plain_seconds": res["plain_seconds_min"], "learned_seconds": res["learned"]["seconds"],
+           "plain_path": res["plain_path"], "k_avg_plain_mean": res["plain_k_avg_mean"],
+           "k_avg_plain_std": res["plain_k_avg_std"], "k_avg_learned": res["learned"]["k_avg"],
+           "k_avg_rel_err": res["k_avg_rel_err"], "droplets_plain": [p_["droplets"] for p_ in res["plain"]],
+           "droplets_learned": res["learned"]["droplets"], "mass_q_drift_learned": res["learned"]["mass_q_drift"],
+           "learned_macro_steps": res["learned"]["learned_macro_steps"],
+           "fallback_spans": res["learned"]["fallback_spans"], "clocks": clocks.summary()}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse_args()
     if args.warmup < 3:
@@ -444,6 +476,8 @@ def main():
         return run_launches(args, w)
     if args.ensemble:
         return run_ensemble(args)
+    if args.learned:
+        return run_learned(args)
     if args.impl == "reference":
         return run_reference_arm(args, w, rank, world)
     import torch
