@@ -213,6 +213,7 @@ class FluxNet:
         z = np.load(path, allow_pickle=False)
         net = cls(device=device)
         net.load_state_dict({k: z[k] for k in z.files})
+        net.K = int(z["K"]) if "K" in z.files else 50
         return net
 
     # -- passes
@@ -281,7 +282,7 @@ def model_params_tensor(models, device):
     return torch.tensor([[m.zeta, m.lamb, m.T] for m in models], dtype=torch.float32, device=device)
 
 
-def generate_pairs(n_traj: int, size: int, K: int, sample_steps, *, dt: float = 1e-3, seed: int = 0,
+def generate_pairs(n_traj: int, size: int, K, sample_steps, *, dt: float = 1e-3, seed: int = 0,
                    graph_steps: int = 50):
     """Training pairs from the plain integrator.
 
@@ -291,7 +292,9 @@ def generate_pairs(n_traj: int, size: int, K: int, sample_steps, *, dt: float = 
     batched ensemble. At each sample step the states are copied into a second, noiseless
     ensemble with the same (zeta, lambda) that runs K steps: the pair is (state, its
     deterministic K-step increment). Returns device tensors phi [S, n, H, W],
-    delta [S, n, H, W] and params [n, 3], and the model list.
+    delta [S, n, H, W] and params [n, 3], and the model list. K may be a list of
+    increasing step counts; delta is then a dict {K: [S, n, H, W]} (one noiseless run
+    per sample, read at each K).
     """
     torch = _torch()
     rng = np.random.default_rng(seed)
@@ -308,20 +311,24 @@ def generate_pairs(n_traj: int, size: int, K: int, sample_steps, *, dt: float = 
     noisy = Ensemble(fields, stencil, models, precision="f32c", seeds=seeds, graph_steps=graph_steps)
     det = Ensemble(fields, stencil, quiet, precision="f32c", seeds=seeds, graph_steps=graph_steps)
     S = len(sample_steps)
+    Ks = sorted(int(k) for k in (K if isinstance(K, (list, tuple)) else [K]))
     phi = torch.empty(S, n_traj, size, size, dtype=torch.float32, device="cuda")
-    delta = torch.empty_like(phi)
+    deltas = {k: torch.empty_like(phi) for k in Ks}
     done = 0
     for s, st in enumerate(sample_steps):
         noisy.run(int(st) - done)
         done = int(st)
         x = noisy.gather(phi[s].reshape(-1))
         det.scatter(x)
-        det.run(K)
-        y = det.gather(delta[s].reshape(-1))
-        delta[s].sub_(phi[s])
-        del y
+        ran = 0
+        for k in Ks:
+            det.run(k - ran)
+            ran = k
+            det.gather(deltas[k][s].reshape(-1))
+            deltas[k][s].sub_(phi[s])
     noisy.close()
     det.close()
+    delta = deltas if isinstance(K, (list, tuple)) else deltas[Ks[0]]
     return phi, delta, model_params_tensor(models, "cuda"), models
 
 
@@ -513,6 +520,8 @@ class LearnedStepper:
         tol: largest accepted relative residual ||learned - plain|| / ||plain - start|| of the
             checked deterministic macro step's increments.
         residual_sigma: if > 0, compare Gaussian low-passed increments (width in sites).
+        atol: floor (RMS per site) on the increment norm the residual is divided by, so that
+            nearly static states are judged by the absolute error of the macro step.
         bound: |phi| above which a state is rejected.
         use_graph: replay the learned macro step from a CUDA graph (captured on first use).
         filter_noise: shape the K-step noise draw with :func:`noise_filter` (the K-step
@@ -522,7 +531,7 @@ class LearnedStepper:
 
     def __init__(self, net: FluxNet, field, stencil, model, *, K: int = 50, seed: int = 0, check_every: int = 20,
                  tol: float = 0.5, bound: float = 3.0, plain_precision: str = "f32", use_graph: bool = True,
-                 filter_noise: bool = True, residual_sigma: float = 0.0):
+                 filter_noise: bool = True, residual_sigma: float = 0.0, atol: float = 0.0):
         torch = _torch()
         self.net = net
         self.stencil = Stencil(stencil)
@@ -533,6 +542,7 @@ class LearnedStepper:
         self.check_every = int(check_every)
         self.tol = float(tol)
         self.bound = float(bound)
+        self.atol = float(atol)
         host = np.asarray(field, dtype=np.float64)
         self.shape = host.shape
         dev = torch.device("cuda")
@@ -645,8 +655,10 @@ class LearnedStepper:
         if self._wres is not None:
             dpred, dplain = lowpass(dpred, self._wres), lowpass(dplain, self._wres)
         num = torch.linalg.vector_norm(dpred - dplain)
-        den = torch.linalg.vector_norm(dplain)
-        res = float((num / torch.clamp(den, min=1e-30)).item())
+        # the increment's norm, floored at atol RMS per site so that near-static states
+        # (tiny increments) are judged by the absolute error
+        den = torch.clamp(torch.linalg.vector_norm(dplain), min=self.atol * math.sqrt(dplain.numel()) + 1e-30)
+        res = float((num / den).item())
         self.residuals.append(res)
         return res <= self.tol and math.isfinite(res)
 
@@ -695,50 +707,59 @@ def torch_round_fix(f):
 DEFAULT_SAMPLE_STEPS = (0, 1000, 3000, 10000, 30000, 100000, 200000, 400000, 700000, 1000000)
 
 
-def train_default(out: str | None = None, *, n_traj: int = 512, size: int = 128, K: int = 50, dt: float = 1e-3,
+def train_default(out: str | None = None, *, n_traj: int = 512, size: int = 128, K=50, dt: float = 1e-3,
                   sample_steps=DEFAULT_SAMPLE_STEPS, iters: int = 8000, batch: int = 16, lr: float = 2e-3,
                   seed: int = 0, holdout: float = 0.1, lowpass_sigma: float = 0.0, highpass_weight: float = 1.0,
-                  log=print) -> tuple[FluxNet, dict]:
-    """Generate pairs with the plain integrator, train a FluxNet on the device kernels,
-    report the held-out error, and optionally save the weights (``FluxNet.load``)."""
+                  log=print):
+    """Generate pairs with the plain integrator, train a FluxNet per K on the device kernels,
+    report the held-out errors, and optionally save the weights (``FluxNet.load``; ``out``
+    may contain ``{K}``). K may be one step count or a list sharing one set of trajectories.
+    Returns {K: (net, info)}."""
     import time
     torch = _torch()
+    Ks = list(K) if isinstance(K, (list, tuple)) else [int(K)]
     t0 = time.perf_counter()
-    phi, delta, params, _ = generate_pairs(n_traj, size, K, sample_steps, dt=dt, seed=seed)
+    phi, deltas, params, _ = generate_pairs(n_traj, size, Ks, sample_steps, dt=dt, seed=seed)
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
     n_test = max(1, int(round(holdout * n_traj)))
-    tr = (phi[:, :-n_test], delta[:, :-n_test], params[:-n_test])
-    te = (phi[:, -n_test:], delta[:, -n_test:], params[-n_test:])
-    net = FluxNet(seed=seed)
-    # the linear part depends on (a, c, kappa, dt, shape) only, which the pair set shares
-    lin = LinearPart((size, size), Stencil(dt, 1, 1), Model(a=-0.25, b=0, c=0.25, kappa=1), K)
-    zero = FluxNet(seed=seed)
-    for w in zero.weights:
-        w.zero_()
-    linear_only = evaluate(zero, *te, K=K, dt=dt, linear=lin)
-    before = evaluate(net, *te, K=K, dt=dt, linear=lin)
-    t1 = time.perf_counter()
-    hist = train(net, *tr, K=K, dt=dt, iters=iters, batch=batch, lr=lr, seed=seed, log_every=max(1, iters // 20),
-                 lowpass_sigma=lowpass_sigma, highpass_weight=highpass_weight, linear=lin)
-    torch.cuda.synchronize()
-    t_train = time.perf_counter() - t1
-    after = evaluate(net, *te, K=K, dt=dt, linear=lin)
-    after_lp = evaluate(net, *te, K=K, dt=dt, lowpass_sigma=2.0, linear=lin)
-    info = {"n_traj": n_traj, "size": size, "K": K, "dt": dt, "sample_steps": list(sample_steps), "iters": iters,
-            "batch": batch, "lr": lr, "seed": seed, "pairs": int(phi.shape[0] * phi.shape[1]),
-            "data_seconds": t_data, "train_seconds": t_train, "heldout_rel_mse_linear_part_only": linear_only,
-            "heldout_rel_mse_untrained": before,
-            "heldout_rel_mse": after, "heldout_rel_mse_lowpass2": after_lp, "lowpass_sigma": lowpass_sigma,
-            "highpass_weight": highpass_weight, "loss_history": hist}
-    if log:
-        log(f"data {t_data:.1f} s, train {t_train:.1f} s, held-out relative MSE: linear part alone "
-            f"{linear_only:.3g}, untrained {before:.3g}, trained {after:.3g} (low-passed {after_lp:.3g})")
-    if out:
-        net.save(out, K=K, dt=dt, heldout_rel_mse=after, heldout_rel_mse_lowpass2=after_lp, iters=iters,
-                 n_traj=n_traj, size=size, lowpass_sigma=lowpass_sigma)
-    del phi, delta
-    return net, info
+    results = {}
+    for k in Ks:
+        delta = deltas[k]
+        tr = (phi[:, :-n_test], delta[:, :-n_test], params[:-n_test])
+        te = (phi[:, -n_test:], delta[:, -n_test:], params[-n_test:])
+        # the linear part depends on (a, c, kappa, dt, K, shape) only, which the pair set shares
+        lin = LinearPart((size, size), Stencil(dt, 1, 1), Model(a=-0.25, b=0, c=0.25, kappa=1), k)
+        zero = FluxNet(seed=seed)
+        for w in zero.weights:
+            w.zero_()
+        linear_only = evaluate(zero, *te, K=k, dt=dt, linear=lin)
+        net = FluxNet(seed=seed)
+        before = evaluate(net, *te, K=k, dt=dt, linear=lin)
+        t1 = time.perf_counter()
+        hist = train(net, *tr, K=k, dt=dt, iters=iters, batch=batch, lr=lr, seed=seed,
+                     log_every=max(1, iters // 20), lowpass_sigma=lowpass_sigma, highpass_weight=highpass_weight,
+                     linear=lin)
+        torch.cuda.synchronize()
+        t_train = time.perf_counter() - t1
+        after = evaluate(net, *te, K=k, dt=dt, linear=lin)
+        after_lp = evaluate(net, *te, K=k, dt=dt, lowpass_sigma=2.0, linear=lin)
+        net.K = k
+        info = {"n_traj": n_traj, "size": size, "K": k, "dt": dt, "sample_steps": list(sample_steps),
+                "iters": iters, "batch": batch, "lr": lr, "seed": seed, "pairs": int(phi.shape[0] * phi.shape[1]),
+                "data_seconds": t_data, "train_seconds": t_train, "heldout_rel_mse_linear_part_only": linear_only,
+                "heldout_rel_mse_untrained": before, "heldout_rel_mse": after,
+                "heldout_rel_mse_lowpass2": after_lp, "lowpass_sigma": lowpass_sigma,
+                "highpass_weight": highpass_weight, "loss_history": hist}
+        if log:
+            log(f"K={k}: data {t_data:.1f} s, train {t_train:.1f} s, held-out relative MSE: linear part alone "
+                f"{linear_only:.3g}, untrained {before:.3g}, trained {after:.3g} (low-passed {after_lp:.3g})")
+        if out:
+            net.save(out.format(K=k), K=k, dt=dt, heldout_rel_mse=after, heldout_rel_mse_lowpass2=after_lp,
+                     iters=iters, n_traj=n_traj, size=size, lowpass_sigma=lowpass_sigma)
+        results[k] = (net, info)
+    del phi, deltas
+    return results
 
 
 def _timed(fn):
@@ -751,9 +772,9 @@ def _timed(fn):
     return time.perf_counter() - t0
 
 
-def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: int = 50, seed: int = 0,
+def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: int | None = None, seed: int = 0,
                        check_every: int = 20, tol: float = 0.5, plain_seeds=(1, 2, 3), residual_sigma: float = 2.0,
-                       filter_noise: bool = True) -> dict:
+                       filter_noise: bool = True, atol: float = 0.0) -> dict:
     """Time to ``t_end`` and end-state statistics of the learned stepper against the plain
     FP32 integrator (the faster of the Integrator and a one-replica CUDA-graph ensemble)
     from the same initial field: S(k) mean wavenumber (the reference notebook's
@@ -761,10 +782,11 @@ def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: 
     show the spread of its statistics."""
     from .analysis import count_droplets, mean_wavenumber, structure_factor
     stencil, model = Stencil(stencil), Model(model)
+    K = int(K if K is not None else getattr(net, "K", 50))
     nsteps = int(round(t_end / stencil.dt))
     field = np.asarray(field, dtype=np.float64)
     phi0 = float(field.mean())
-    res = {"t_end": t_end, "K": K, "shape": list(field.shape), "model": model.as_dict(), "tol": tol,
+    res = {"t_end": t_end, "K": K, "shape": list(field.shape), "model": model.as_dict(), "tol": tol, "atol": atol,
            "check_every": check_every, "residual_sigma": residual_sigma, "filter_noise": filter_noise, "plain": []}
     probe = max(1, min(nsteps, 20000))
     sim = Integrator(field, stencil, model, precision="f32", seed=0)
@@ -793,7 +815,7 @@ def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: 
                              "k_peak": float(k[np.nanargmax(S)]), "droplets": count_droplets(f, phi0),
                              "mass_drift": float(f.sum() - field.sum())})
     st = LearnedStepper(net, field, stencil, model, K=K, seed=seed, check_every=check_every, tol=tol,
-                        residual_sigma=residual_sigma, filter_noise=filter_noise)
+                        residual_sigma=residual_sigma, filter_noise=filter_noise, atol=atol)
     m0 = st.mass_q()
     sec = _timed(lambda: st.run_for_time(t_end))
     f = st.field
@@ -818,7 +840,8 @@ def _main(argv=None) -> int:
     ap = argparse.ArgumentParser(prog="python -m activemodelbplus.learned")
     sub = ap.add_subparsers(dest="cmd", required=True)
     t = sub.add_parser("train", help="generate pairs with the plain integrator and train the flux network")
-    t.add_argument("--out", required=True)
+    t.add_argument("--out", required=True, help="weights path; may contain {K}")
+    t.add_argument("--K", default="50", help="Euler steps per macro step; comma-separated for several")
     t.add_argument("--n-traj", type=int, default=512)
     t.add_argument("--size", type=int, default=128)
     t.add_argument("--iters", type=int, default=8000)
@@ -840,15 +863,18 @@ def _main(argv=None) -> int:
     c.add_argument("--residual-sigma", type=float, default=2.0)
     c.add_argument("--no-noise-filter", action="store_true")
     c.add_argument("--plain-seeds", default="1,2,3")
+    c.add_argument("--atol", type=float, default=0.0)
     a = ap.parse_args(argv)
     if a.cmd == "train":
         steps = [int(v) for v in a.sample_steps.split(",")]
-        _, info = train_default(a.out, n_traj=a.n_traj, size=a.size, iters=a.iters, batch=a.batch, lr=a.lr,
-                                seed=a.seed, sample_steps=steps, lowpass_sigma=a.lowpass_sigma,
-                                highpass_weight=a.highpass_weight)
+        Ks = [int(v) for v in a.K.split(",")]
+        res = train_default(a.out, n_traj=a.n_traj, size=a.size, iters=a.iters, batch=a.batch, lr=a.lr,
+                            seed=a.seed, sample_steps=steps, lowpass_sigma=a.lowpass_sigma,
+                            highpass_weight=a.highpass_weight, K=Ks if len(Ks) > 1 else Ks[0])
         if a.info:
-            with open(a.info, "w") as fh:
-                json.dump(info, fh, indent=1)
+            for k, (_, info) in res.items():
+                with open(a.info.format(K=k), "w") as fh:
+                    json.dump(info, fh, indent=1)
         return 0
     net = FluxNet.load(a.weights)
     rng = np.random.default_rng(a.seed)
@@ -856,7 +882,7 @@ def _main(argv=None) -> int:
     model = Model(a=-0.25, b=0, c=0.25, kappa=1, lamb=-1, zeta=-4, T=a.temperature)
     res = compare_with_plain(net, field, Stencil(1e-3, 1, 1), model, t_end=a.t_end, seed=a.seed,
                              check_every=a.check_every, tol=a.tol, residual_sigma=a.residual_sigma,
-                             filter_noise=not a.no_noise_filter,
+                             filter_noise=not a.no_noise_filter, atol=a.atol,
                              plain_seeds=tuple(int(v) for v in a.plain_seeds.split(",")))
     print(json.dumps(res))
     return 0
