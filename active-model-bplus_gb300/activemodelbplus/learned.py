@@ -465,25 +465,32 @@ def noise_filter(shape, stencil, model, K: int, curvature: float | None = None):
 
 
 class LinearPart:
-    """The stiff linear part of K plain steps, applied exactly and written as a face flux.
+    """The stiff linear part of K plain steps, applied exactly and written as a face flux,
+    and the K-step noise as a face flux.
 
     K explicit steps of the scheme linearised about the bulk multiply mode k by
     E(k) = a(k)^K. The face flux G with (face-difference) divergence
     div G = -(E - 1) phi / (K dt) is G_hat = -(E - 1) phi_hat conj(d) / (|d_x|^2 + |d_y|^2) / (K dt)
     per component, d_x = (1 - exp(-i k_x dx)) / dx the symbol of the face difference (zero
     at k = 0, where E = 1). Adding G to the network's flux makes a macro step propagate the
-    linear part exactly (in particular the fast decay of short-wavelength fluctuations,
-    which matches the noise_filter draw), and, as a flux, it keeps the fixed-point update
-    exactly conservative. FFTs are cuFFT calls through torch.
+    linear part exactly (in particular the fast decay of short-wavelength fluctuations), and,
+    as a flux, it keeps the fixed-point update exactly conservative.
+
+    The noise of a macro step is noise_mag * W8 (g * xi) per component: one Philox draw xi,
+    shaped by the noise_filter g and turned into face fluxes by the order-8 face sums W8 (the
+    D8 derivative of the plain scheme's noise as a face difference). Both are linear filters,
+    so ``extra`` forms linear part + noise with one inverse FFT per component (cuFFT through
+    torch). ``with_linear=False`` keeps only the noise.
     """
 
-    def __init__(self, shape, stencil, model, K: int, device=None, curvature: float | None = None):
+    def __init__(self, shape, stencil, model, K: int, device=None, curvature: float | None = None,
+                 with_linear: bool = True):
         torch = _torch()
         st = Stencil(stencil)
         ny, nx = shape
         self.shape = (ny, nx)
         a = 1.0 - st.dt * linear_rate(shape, st, model, curvature)
-        e1 = a ** K - 1.0
+        e1 = (a ** K - 1.0) if with_linear else np.zeros_like(a)
         ty = 2 * np.pi * np.fft.fftfreq(ny)[:, None]
         tx = 2 * np.pi * np.fft.rfftfreq(nx)[None, :]
         dxs = (1.0 - np.exp(-1j * tx)) / st.dx
@@ -495,17 +502,44 @@ class LinearPart:
         my = -e1 * np.conj(dys) / den / dtk
         mx[0, 0] = 0.0
         my[0, 0] = 0.0
+        g = noise_filter(shape, st, model, K, curvature).numpy().astype(np.float64)
+        c = (4.0 / 5.0, -1.0 / 5.0, 4.0 / 105.0, -1.0 / 280.0)
+        w8 = [sum(c[d - 1] for d in range(max(e, 1 - e), 5)) for e in range(-3, 5)]
+        # F(j + 1/2) = sum_e w_e xi(j + e)  <->  F_hat = xi_hat * sum_e w_e exp(i k e)
+        sym_x = sum(w * np.exp(1j * tx * e) for w, e in zip(w8, range(-3, 5)))
+        sym_y = sum(w * np.exp(1j * ty * e) for w, e in zip(w8, range(-3, 5)))
         dev = device if device is not None else "cuda"
-        self.my = torch.from_numpy(np.broadcast_to(my, (ny, nx // 2 + 1)).astype(np.complex64)).to(dev)
-        self.mx = torch.from_numpy(np.broadcast_to(mx, (ny, nx // 2 + 1)).astype(np.complex64)).to(dev)
+        full = (ny, nx // 2 + 1)
+        self.my = torch.from_numpy(np.broadcast_to(my, full).astype(np.complex64)).to(dev)
+        self.mx = torch.from_numpy(np.broadcast_to(mx, full).astype(np.complex64)).to(dev)
+        self.ny_ = torch.from_numpy(np.broadcast_to(g * sym_y, full).astype(np.complex64)).to(dev)
+        self.nx_ = torch.from_numpy(np.broadcast_to(g * sym_x, full).astype(np.complex64)).to(dev)
 
     def flux(self, phi):
-        """phi [B, H, W] -> G [B, 2, H, W] (component 0 = y face, 1 = x face)."""
+        """Linear part only: phi [B, H, W] -> G [B, 2, H, W] (component 0 = y face, 1 = x face)."""
         torch = _torch()
         spec = torch.fft.rfft2(phi)
         gy = torch.fft.irfft2(spec * self.my, s=self.shape)
         gx = torch.fft.irfft2(spec * self.mx, s=self.shape)
         return torch.stack([gy, gx], dim=1)
+
+    def extra(self, phi, xi, noise_mag: float, out):
+        """Linear part of phi [H, W] plus the noise flux of xi [2, H, W] (or None) into out [2, H, W]:
+        forward FFTs, one combining kernel (``amb_learned_spectral_combine``), two inverse FFTs."""
+        torch = _torch()
+        # cuFFT through torch may return the spectrum in a transposed (column-major) layout;
+        # the combining kernel reads row-major arrays
+        spec = torch.fft.rfft2(phi).contiguous()
+        sxi = torch.fft.rfft2(xi).contiguous() if xi is not None else None
+        if not spec.is_cuda:
+            raise CudaException("LinearPart.extra runs on the GPU")
+        comb = torch.empty((2,) + tuple(spec.shape), dtype=spec.dtype, device=spec.device)
+        _check(N.lib().amb_learned_spectral_combine(
+            _ptr(spec), _ptr(sxi), _ptr(self.my), _ptr(self.mx), _ptr(self.ny_), _ptr(self.nx_),
+            float(noise_mag), spec.numel(), _ptr(comb[0]), _ptr(comb[1]), _stream()))
+        torch.fft.irfft2(comb[0], s=self.shape, out=out[0])
+        torch.fft.irfft2(comb[1], s=self.shape, out=out[1])
+        return out
 
 
 class LearnedStepper:
@@ -557,7 +591,9 @@ class LearnedStepper:
         self.fallback_spans = 0
         self.residuals = []
         self._g = noise_filter(self.shape, self.stencil, self.model, self.K).to(dev) if filter_noise else None
-        self._linear = LinearPart(self.shape, self.stencil, self.model, self.K, dev) if net.linear_split else None
+        self._linear = LinearPart(self.shape, self.stencil, self.model, self.K, dev,
+                                  with_linear=bool(getattr(net, "linear_split", False)))
+        self._extra = torch.zeros(2, *self.shape, dtype=torch.float32, device=dev)
         self._wres = lowpass_weights(self.shape, residual_sigma, dev) if residual_sigma > 0 else None
         self.use_graph = bool(use_graph)
         self._graph = None
@@ -579,23 +615,32 @@ class LearnedStepper:
         return int(self.phi_q.to(dtype=_torch().int64).sum().item())
 
     def _flux(self):
+        """Deterministic flux of a macro step from the current state (network + linear part)."""
         flux = self.net.forward(network_input(self.phi_f.unsqueeze(0), self.params))
-        if self._linear is not None:
+        if getattr(self.net, "linear_split", False):
             flux = flux + self._linear.flux(self.phi_f.unsqueeze(0))
         return flux
 
-    def _apply(self, flux, noisy: bool) -> None:
+    def _apply(self, noisy: bool) -> None:
+        """Network flux, plus (one spectral pass) the linear part and the filtered noise flux,
+        then the exactly conservative fixed-point update."""
         torch = _torch()
         lib = N.lib()
         ny, nx = self.shape
-        xi, mag = None, 0.0
-        if noisy and self.model.T > 0:
+        net_flux = self.net.forward(network_input(self.phi_f.unsqueeze(0), self.params))
+        noisy = noisy and self.model.T > 0
+        if noisy:
             _check(lib.amb_learned_noise(ny, nx, self.seed, _ptr(self.step_dev), _ptr(self.xi), _stream()))
-            if self._g is not None:
-                self.xi.copy_(torch.fft.irfft2(torch.fft.rfft2(self.xi) * self._g, s=(ny, nx)))
-            xi = self.xi
-            mag = math.sqrt(2.0 * self.model.T) * math.sqrt(1.0 / (self.dtk * self.stencil.dx * self.stencil.dy))
-        _check(lib.amb_learned_update(_ptr(flux), ny, nx, self.dtk, self.stencil.dx, self.stencil.dy, _ptr(xi), mag,
+        mag = math.sqrt(2.0 * self.model.T) * math.sqrt(1.0 / (self.dtk * self.stencil.dx * self.stencil.dy))
+        xi_direct = None
+        if self._g is None and noisy:
+            # unfiltered noise: the update kernel forms the face sums of xi itself
+            self._linear.extra(self.phi_f, None, 0.0, self._extra)
+            xi_direct = self.xi
+        else:
+            self._linear.extra(self.phi_f, self.xi if noisy else None, mag, self._extra)
+        _check(lib.amb_learned_update(_ptr(net_flux), _ptr(self._extra), ny, nx, self.dtk, self.stencil.dx,
+                                      self.stencil.dy, _ptr(xi_direct), mag if xi_direct is not None else 0.0,
                                       _ptr(self.phi_q), _ptr(self.phi_f), self.bound, _ptr(self.flag), _stream()))
         self.step_dev.add_(1)
 
@@ -611,7 +656,7 @@ class LearnedStepper:
             side = torch.cuda.Stream()
             side.wait_stream(torch.cuda.current_stream())
             with torch.cuda.stream(side):  # one eager pass first: allocator pools, cuFFT plans
-                self._apply(self._flux(), noisy=noisy)
+                self._apply(noisy=noisy)
             torch.cuda.current_stream().wait_stream(side)
             self.phi_q.copy_(saved[0])
             self.phi_f.copy_((self.phi_q.double() / FIX).float())
@@ -619,12 +664,12 @@ class LearnedStepper:
             self.flag.copy_(saved[2])
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g):  # records only; the state changes at replay
-                self._apply(self._flux(), noisy=noisy)
+                self._apply(noisy=noisy)
             self._graph = g
         if self._graph is not None:
             self._graph.replay()
         else:
-            self._apply(self._flux(), noisy=noisy)
+            self._apply(noisy=noisy)
 
     def _set_from_float(self, f) -> None:
         self.phi_q.copy_(torch_round_fix(f))

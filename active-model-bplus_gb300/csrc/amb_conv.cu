@@ -692,63 +692,72 @@ namespace
         }
     }
 
-    // Face weights of the order-8 central derivative written as a difference of
-    // face sums: D8 f(j) = F(j + 1/2) - F(j - 1/2) with F(j + 1/2) = sum_e w_e f(j + e),
-    // e = -3..4, w_e = sum of c_d over d >= max(e, 1 - e), c = (4/5, -1/5, 4/105, -1/280).
-    __device__ __forceinline__ double d8_face_weight(int e)
+    // Face weights of the order-8 central derivative written as a difference of face sums:
+    // D8 f(j) = F(j + 1/2) - F(j - 1/2) with F(j + 1/2) = sum_e w_e f(j + e), e = -3..4,
+    // w_e = sum of c_d over d >= max(e, 1 - e), c = (4/5, -1/5, 4/105, -1/280) (the sum in
+    // double, in increasing d, then rounded to float).
+    constexpr double kC1 = 4.0 / 5.0, kC2 = -1.0 / 5.0, kC3 = 4.0 / 105.0, kC4 = -1.0 / 280.0;
+
+    __device__ __forceinline__ float d8_face_weight(int e)
     {
         const int d0 = e > 1 - e ? e : 1 - e;
-        const double c[4] = {4.0 / 5.0, -1.0 / 5.0, 4.0 / 105.0, -1.0 / 280.0};
-        double w = 0.0;
-        for (int d = d0; d <= 4; ++d) w += c[d - 1];
-        return w;
+        return d0 == 1 ? float(kC1 + kC2 + kC3 + kC4)
+                       : d0 == 2 ? float(kC2 + kC3 + kC4) : d0 == 3 ? float(kC3 + kC4) : float(kC4);
     }
 
-    // Integer face increment through the face after site (r, c) along the axis (dr, dc).
-    __device__ __forceinline__ long long face_q(const float* __restrict__ f, const float* __restrict__ xi,
-                                                double noise_mag, double scale, int r, int c, int dr, int dc,
-                                                int nrows, int ncols)
+    // Integer face increment through the face after site (r, c) along the axis (dr, dc), in
+    // FP32 with explicitly rounded operations, so the two sites sharing the face compute the
+    // same integer.
+    __device__ __forceinline__ long long face_q(const float* __restrict__ f, const float* __restrict__ extra,
+                                                const float* __restrict__ xi, float noise_mag, float scale, int r,
+                                                int c, int dr, int dc, int nrows, int ncols)
     {
-        double v = double(f[size_t(r) * ncols + c]);
+        const size_t k = size_t(r) * ncols + c;
+        float v = f[k];
+        if (extra) v = __fadd_rn(v, extra[k]);
         if (xi)
         {
-            double s = 0.0;
+            float s = 0.f;
+#pragma unroll
             for (int e = -3; e <= 4; ++e)
             {
                 int rr = r + dr * e, cc = c + dc * e;
                 rr = rr < 0 ? rr + nrows : (rr >= nrows ? rr - nrows : rr);
                 cc = cc < 0 ? cc + ncols : (cc >= ncols ? cc - ncols : cc);
-                s = __dadd_rn(s, __dmul_rn(d8_face_weight(e), double(xi[size_t(rr) * ncols + cc])));
+                s = __fadd_rn(s, __fmul_rn(d8_face_weight(e), xi[size_t(rr) * ncols + cc]));
             }
-            v = __dadd_rn(v, __dmul_rn(noise_mag, s));
+            v = __fadd_rn(v, __fmul_rn(noise_mag, s));
         }
-        double q = __dmul_rn(scale, v);
-        q = q > 1e9 ? 1e9 : (q < -1e9 ? -1e9 : q);
-        return llrint(q);
+        float q = __fmul_rn(scale, v);
+        q = q > 1e9f ? 1e9f : (q < -1e9f ? -1e9f : q);
+        return __float2ll_rn(q);
     }
 
     // phi_q -= sum of integer face increments (each face computed identically by the two
     // sites that share it, so the sum over all sites is unchanged: exact conservation).
-    __global__ void learned_update_kernel(const float* __restrict__ flux, const float* __restrict__ xi, int nrows,
-                                          int ncols, double scale_y, double scale_x, double noise_mag,
-                                          int32_t* __restrict__ phi_q, float* __restrict__ phi_f, long long bound,
-                                          int* __restrict__ flag)
+    __global__ void learned_update_kernel(const float* __restrict__ flux, const float* __restrict__ extra,
+                                          const float* __restrict__ xi, int nrows, int ncols, float scale_y,
+                                          float scale_x, float noise_mag, int32_t* __restrict__ phi_q,
+                                          float* __restrict__ phi_f, long long bound, int* __restrict__ flag)
     {
         const size_t plane = size_t(nrows) * ncols;
         const float* fy = flux;
         const float* fx = flux + plane;
+        const float* ey = extra;
+        const float* ex = extra ? extra + plane : nullptr;
         const float* xy = xi;
         const float* xx = xi ? xi + plane : nullptr;
         for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < plane; i += size_t(gridDim.x) * blockDim.x)
         {
             const int r = int(i / ncols), c = int(i - size_t(r) * ncols);
             const int rm = r == 0 ? nrows - 1 : r - 1, cm = c == 0 ? ncols - 1 : c - 1;
-            long long dq = face_q(fx, xx, noise_mag, scale_x, r, c, 0, 1, nrows, ncols) -
-                           face_q(fx, xx, noise_mag, scale_x, r, cm, 0, 1, nrows, ncols) +
-                           face_q(fy, xy, noise_mag, scale_y, r, c, 1, 0, nrows, ncols) -
-                           face_q(fy, xy, noise_mag, scale_y, rm, c, 1, 0, nrows, ncols);
+            long long dq = face_q(fx, ex, xx, noise_mag, scale_x, r, c, 0, 1, nrows, ncols) -
+                           face_q(fx, ex, xx, noise_mag, scale_x, r, cm, 0, 1, nrows, ncols) +
+                           face_q(fy, ey, xy, noise_mag, scale_y, r, c, 1, 0, nrows, ncols) -
+                           face_q(fy, ey, xy, noise_mag, scale_y, rm, c, 1, 0, nrows, ncols);
             long long q = (long long)phi_q[i] - dq;
-            const bool bad = !isfinite(fx[i]) || !isfinite(fy[i]) || q > bound || q < -bound;
+            bool bad = !isfinite(fx[i]) || !isfinite(fy[i]) || q > bound || q < -bound;
+            if (extra) bad = bad || !isfinite(ex[i]) || !isfinite(ey[i]);
             if (bad)
             {
                 atomicOr(flag, 1);
@@ -756,6 +765,32 @@ namespace
             }
             phi_q[i] = int32_t(q);
             phi_f[i] = float(double(q) * (1.0 / 16777216.0));
+        }
+    }
+
+    // out_c = phi_hat * m_c + noise_mag * xi_hat_c * n_c for c = y, x (complex rfft2 spectra,
+    // [ny][nx/2+1] each; xi_hat may be null).
+    __global__ void spectral_combine_kernel(const float2* __restrict__ phi_hat, const float2* __restrict__ xi_hat,
+                                            const float2* __restrict__ my, const float2* __restrict__ mx,
+                                            const float2* __restrict__ ny_, const float2* __restrict__ nx_,
+                                            float noise_mag, size_t n, float2* __restrict__ out_y,
+                                            float2* __restrict__ out_x)
+    {
+        for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+        {
+            const float2 p = phi_hat[i], a = my[i], b = mx[i];
+            float2 y = make_float2(p.x * a.x - p.y * a.y, p.x * a.y + p.y * a.x);
+            float2 x = make_float2(p.x * b.x - p.y * b.y, p.x * b.y + p.y * b.x);
+            if (xi_hat)
+            {
+                const float2 u = xi_hat[i], v = xi_hat[n + i], c = ny_[i], d = nx_[i];
+                y.x += noise_mag * (u.x * c.x - u.y * c.y);
+                y.y += noise_mag * (u.x * c.y + u.y * c.x);
+                x.x += noise_mag * (v.x * d.x - v.y * d.y);
+                x.y += noise_mag * (v.x * d.y + v.y * d.x);
+            }
+            out_y[i] = y;
+            out_x[i] = x;
         }
     }
 
@@ -970,9 +1005,9 @@ extern "C" int amb_learned_noise(int nrows, int ncols, uint64_t seed, const int6
     return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_noise", e);
 }
 
-extern "C" int amb_learned_update(const float* flux, int nrows, int ncols, double dt_macro, double dx, double dy,
-                                  const float* xi, double noise_mag, int32_t* phi_q, float* phi_f, double bound,
-                                  int* flag, void* stream)
+extern "C" int amb_learned_update(const float* flux, const float* extra, int nrows, int ncols, double dt_macro,
+                                  double dx, double dy, const float* xi, double noise_mag, int32_t* phi_q,
+                                  float* phi_f, double bound, int* flag, void* stream)
 {
     if (!flux || !phi_q || !phi_f || !flag || nrows < 1 || ncols < 1 || !(dt_macro > 0) || !(dx > 0) ||
         !(dy > 0) || !(noise_mag >= 0) || !(bound > 0))
@@ -983,9 +1018,24 @@ extern "C" int amb_learned_update(const float* flux, int nrows, int ncols, doubl
     const double fix = 16777216.0;
     const double qb = std::min(bound * fix, 2.0e9);
     const bool noisy = xi && noise_mag > 0;
-    learned_update_kernel<<<grid, 256, 0, s>>>(flux, noisy ? xi : nullptr, nrows, ncols, dt_macro / dy * fix,
-                                               dt_macro / dx * fix, noisy ? noise_mag : 0.0, phi_q, phi_f,
-                                               (long long)qb, flag);
+    learned_update_kernel<<<grid, 256, 0, s>>>(flux, extra, noisy ? xi : nullptr, nrows, ncols,
+                                               float(dt_macro / dy * fix), float(dt_macro / dx * fix),
+                                               noisy ? float(noise_mag) : 0.f, phi_q, phi_f, (long long)qb, flag);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_update", e);
+}
+
+extern "C" int amb_learned_spectral_combine(const void* phi_hat, const void* xi_hat, const void* my, const void* mx,
+                                            const void* ny, const void* nx, double noise_mag, int64_t n,
+                                            void* out_y, void* out_x, void* stream)
+{
+    if (!phi_hat || !my || !mx || !out_y || !out_x || n < 1 || (xi_hat && (!ny || !nx)))
+        return fail_invalid("amb_learned_spectral_combine: bad arguments");
+    const int grid = int(std::min<int64_t>((n + 255) / 256, int64_t(sm_count()) * 8));
+    spectral_combine_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const float2*>(phi_hat), static_cast<const float2*>(xi_hat), static_cast<const float2*>(my),
+        static_cast<const float2*>(mx), static_cast<const float2*>(ny), static_cast<const float2*>(nx),
+        float(noise_mag), size_t(n), static_cast<float2*>(out_y), static_cast<float2*>(out_x));
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_spectral_combine", e);
 }

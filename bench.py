@@ -356,7 +356,8 @@ def run_ours(args, w, rank, world, dist):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "f64" else "f32", "data": "synthetic", "config": config_of(args, w),
+        "dtype": "f64" if args.precision == "f64" else "f32", "data": "synthetic",
+        "config": dict(config_of(args, w), kernel_config=sim.kernel_config),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s", "traffic": measured_traffic(args),

@@ -291,17 +291,24 @@ int amb_learned_input(const float* phi, const float* params, int batch, int nrow
 int amb_learned_noise(int nrows, int ncols, uint64_t seed, const int64_t* step, float* xi, void* stream);
 
 /* One macro step of the learned stepper on a fixed-point field phi_q (int32, phi * 2^24):
- * phi -= dt_macro * div F, F = flux + noise flux, with div the face difference
- * (F_x(r,c) - F_x(r,c-1))/dx + (F_y(r,c) - F_y(r-1,c))/dy. flux: [2][nrows][ncols] FP32
- * (component 0 = y face after (r,c), 1 = x face). If xi is non-NULL the noise flux is the
- * order-8 central derivative of noise_mag * xi written as face sums (xi as from
- * amb_learned_noise, possibly filtered by the caller). Every face increment is rounded to an
- * integer once and applied with opposite signs to its two sites, so sum(phi_q) is conserved
- * exactly. phi_f receives phi_q * 2^-24. *flag |= 1 if the flux is non-finite or |phi|
- * exceeds bound (then clamped). */
-int amb_learned_update(const float* flux, int nrows, int ncols, double dt_macro, double dx, double dy,
-                       const float* xi, double noise_mag, int32_t* phi_q, float* phi_f, double bound, int* flag,
-                       void* stream);
+ * phi -= dt_macro * div F with div the face difference
+ * (F_x(r,c) - F_x(r,c-1))/dx + (F_y(r,c) - F_y(r-1,c))/dy. F = flux + extra (extra may be
+ * NULL), both [2][nrows][ncols] FP32 (component 0 = y face after (r,c), 1 = x face), plus, if
+ * xi is non-NULL, the order-8 central derivative of noise_mag * xi written as face sums (xi as
+ * from amb_learned_noise). Face values are formed in FP32 with explicitly rounded operations,
+ * scaled by dt_macro/d * 2^24 and rounded to an integer once; each face increment is applied
+ * with opposite signs to its two sites, so sum(phi_q) is conserved exactly. phi_f receives
+ * phi_q * 2^-24. *flag |= 1 if a flux is non-finite or |phi| exceeds bound (then clamped). */
+int amb_learned_update(const float* flux, const float* extra, int nrows, int ncols, double dt_macro, double dx,
+                       double dy, const float* xi, double noise_mag, int32_t* phi_q, float* phi_f, double bound,
+                       int* flag, void* stream);
+
+/* Spectral step of the learned stepper's linear part and noise: for n complex rfft2 modes
+ * (complex64 arrays), out_y = phi_hat * my + noise_mag * xi_hat_y * ny and
+ * out_x = phi_hat * mx + noise_mag * xi_hat_x * nx, xi_hat = [2][n] (y then x) or NULL. */
+int amb_learned_spectral_combine(const void* phi_hat, const void* xi_hat, const void* my, const void* mx,
+                                 const void* ny, const void* nx, double noise_mag, int64_t n, void* out_y,
+                                 void* out_x, void* stream);
 
 #ifdef __cplusplus
 }

@@ -10,8 +10,8 @@ has no learned component), so its oracle is the mathematics it implements:
 * its data and weight gradients (torch autograd in float64);
 * GELU in its tanh form (Hendrycks and Gimpel) and its derivative;
 * the face-flux update in int64 fixed point (phi * 2^24), restated with the
-  same IEEE double operations as the device kernel (product, then round half to
-  even), so it is bit-exact at T = 0;
+  same IEEE single-precision operations in the same order as the device kernel
+  (sums, product, then round half to even), so it is bit-exact;
 * the order-8 central difference written as a difference of face sums, from
   the coefficients c = (4/5, -1/5, 4/105, -1/280) of the reference's D8
   operator (src/finite_difference.h:73).
@@ -140,22 +140,29 @@ def d8_face_weights():
     return np.array(out)
 
 
-def face_update(phi_q, flux, dtk, dx=1.0, dy=1.0, xi=None, noise_mag=0.0):
-    """Fixed-point macro step: phi_q (int64 [H, W]) minus the integer face increments of
-    flux [2, H, W] (component 0 = y face after (r, c), 1 = x face), optionally plus the
-    noise flux noise_mag * sum_e w_e xi(. + e) on each face (xi [2, H, W])."""
-    flux = np.asarray(flux, dtype=np.float32).astype(np.float64)
-    w = d8_face_weights()
+def face_update(phi_q, flux, dtk, dx=1.0, dy=1.0, xi=None, noise_mag=0.0, extra=None):
+    """Fixed-point macro step: phi_q (int64 [H, W]) minus the integer face increments of the
+    face flux [2, H, W] (component 0 = y face after (r, c), 1 = x face), plus extra [2, H, W] if
+    given, plus the noise flux noise_mag * sum_e w_e xi(. + e) on each face (xi [2, H, W]).
+    Face values are formed in float32 with the device's operation order (flux + extra, noise
+    sum in increasing e, then times noise_mag, then times the scale dtk / d * 2^24), clamped to
+    +-1e9 and rounded half to even."""
+    f32 = np.float32
+    flux = np.asarray(flux, dtype=f32)
+    w = d8_face_weights().astype(f32)
 
     def faces(comp, axis, scale):
         v = flux[comp].copy()
+        if extra is not None:
+            v = (v + np.asarray(extra[comp], dtype=f32)).astype(f32)
         if xi is not None:
-            x = np.asarray(xi[comp], dtype=np.float32).astype(np.float64)
+            x = np.asarray(xi[comp], dtype=f32)
             s = np.zeros_like(v)
             for i, e in enumerate(range(-3, 5)):
-                s = s + w[i] * np.roll(x, -e, axis=axis)
-            v = v + noise_mag * s
-        q = np.clip(scale * v, -1e9, 1e9)
+                s = (s + (w[i] * np.roll(x, -e, axis=axis)).astype(f32)).astype(f32)
+            v = (v + (f32(noise_mag) * s).astype(f32)).astype(f32)
+        q = (f32(scale) * v).astype(f32)
+        q = np.clip(q, f32(-1e9), f32(1e9))
         return np.rint(q).astype(np.int64)
 
     qy = faces(0, 0, dtk / dy * FIX)

@@ -211,13 +211,16 @@ def test_network_forward_and_gradients_match_oracle():
 
 # ------------------------------------------------------------ fixed-point update
 
-@pytest.mark.parametrize("T", [0.0, 0.05])
-def test_update_is_exact_and_conservative(T):
+@pytest.mark.parametrize("T,with_extra", [(0.0, False), (0.05, False), (0.0, True), (0.05, True)])
+def test_update_is_exact_and_conservative(T, with_extra):
+    """The fixed-point update against the float32 restatement in the oracle: bit-exact, and
+    the integer mass is unchanged."""
     torch, L, N = mods()
     rng = np.random.default_rng(6)
     H, W = 48, 128
     phi_q = np.rint(rng.uniform(-0.8, 0.8, (H, W)) * OL.FIX).astype(np.int32)
     flux = (0.3 * rng.standard_normal((2, H, W))).astype(np.float32)
+    extra = (0.2 * rng.standard_normal((2, H, W))).astype(np.float32) if with_extra else None
     q = torch.from_numpy(phi_q).cuda()
     f = torch.empty(H, W, dtype=torch.float32, device="cuda")
     xi = torch.empty(2, H, W, dtype=torch.float32, device="cuda")
@@ -225,21 +228,23 @@ def test_update_is_exact_and_conservative(T):
     flag = torch.zeros(1, dtype=torch.int32, device="cuda")
     dtk = 0.05
     flux_dev = torch.from_numpy(flux).cuda()
+    extra_dev = torch.from_numpy(extra).cuda() if with_extra else None
     lib, strm = N.lib(), torch.cuda.current_stream().cuda_stream
     mag = math.sqrt(2 * T) * math.sqrt(1 / (dtk * 1.0 * 1.0))
     if T > 0:
         assert lib.amb_learned_noise(H, W, 99, step.data_ptr(), xi.data_ptr(), strm) == 0, N.last_error()
-    rc = lib.amb_learned_update(flux_dev.data_ptr(), H, W, dtk, 1.0, 1.0, xi.data_ptr() if T > 0 else None, mag,
-                                q.data_ptr(), f.data_ptr(), 3.0, flag.data_ptr(), strm)
+    rc = lib.amb_learned_update(flux_dev.data_ptr(), extra_dev.data_ptr() if with_extra else None, H, W, dtk, 1.0,
+                                1.0, xi.data_ptr() if T > 0 else None, mag, q.data_ptr(), f.data_ptr(), 3.0,
+                                flag.data_ptr(), strm)
     assert rc == 0, N.last_error()
     got = q.cpu().numpy().astype(np.int64)
     if T > 0:
-        ref = OL.face_update(phi_q, flux, dtk, xi=xi.cpu().numpy(), noise_mag=mag)
+        ref = OL.face_update(phi_q, flux, dtk, xi=xi.cpu().numpy(), noise_mag=mag, extra=extra)
         import oracle
         xy, xx = oracle.normals(H, W, 99, 7)  # the same Philox-keyed normals, evaluated in double
         assert np.abs(xi.cpu().numpy() - np.stack([xy, xx])).max() < 5e-5
     else:
-        ref = OL.face_update(phi_q, flux, dtk)
+        ref = OL.face_update(phi_q, flux, dtk, extra=extra)
     assert np.array_equal(got, ref)
     assert got.sum() == phi_q.astype(np.int64).sum()
     assert np.array_equal(f.cpu().numpy(), (got / OL.FIX).astype(np.float32))
@@ -249,13 +254,15 @@ def test_update_is_exact_and_conservative(T):
 # ------------------------------------------------------------ stepper and training gain
 
 def test_stepper_conserves_and_falls_back():
-    """An untrained network fails the residual check, so every span is redone by the plain
-    integrator; the fixed-point mass is unchanged by learned macro steps."""
+    """A network whose flux is far off fails the residual check, so every span is redone by
+    the plain integrator; the fixed-point mass is unchanged by learned macro steps."""
     torch, L, N = mods()
     from activemodelbplus.integrator import Model, Stencil
     rng = np.random.default_rng(7)
     field = -0.4 + 0.01 * rng.standard_normal((64, 128))
     net = L.FluxNet(seed=3)
+    net.weights[-1].mul_(100.0)  # a wildly wrong flux on top of the exact linear part
+    net.refresh()
     st = L.LearnedStepper(net, field, Stencil(1e-3, 1, 1), Model(-0.25, 0, 0.25, 1, -1, -4, 0.0), K=50,
                           check_every=4, tol=0.05)
     m0 = st.mass_q()
@@ -268,6 +275,26 @@ def test_stepper_conserves_and_falls_back():
     assert st.learned_steps == 8
     assert st.mass_q() == m1
     assert abs(m1 - m0) < 64 * 128  # plain FP32 spans conserve to rounding
+
+
+def test_linear_macro_step_matches_the_propagator():
+    """With a zero network flux and T = 0, a learned macro step is the linear part alone: the
+    field becomes irfft2(a(k)^K phi_hat) up to the fixed-point rounding (2^-24 per face)."""
+    torch, L, N = mods()
+    from activemodelbplus.integrator import Model, Stencil
+    H, W, K = 64, 256, 50
+    st_, m = Stencil(1e-3, 1, 1), Model(-0.25, 0, 0.25, 1, 0, 0, 0.0)
+    field = 0.3 * np.random.default_rng(8).standard_normal((H, W))
+    net = L.FluxNet(seed=0)
+    net.weights[-1].zero_()
+    net.biases[-1].zero_()
+    s = L.LearnedStepper(net, field, st_, m, K=K, check_every=1, tol=1e9, use_graph=False)
+    start = s.field
+    s._apply(noisy=False)
+    a = (1 - st_.dt * L.linear_rate((H, W), st_, m)) ** K
+    ref = np.fft.irfft2(np.fft.rfft2(start) * a, s=(H, W))
+    assert np.abs(s.field - ref).max() < 1e-5
+    assert s.mass_q() == int(np.rint(start * L.FIX).astype(np.int64).sum())
 
 
 def test_training_gains_over_untrained_and_naive_coarse_step():
@@ -363,3 +390,26 @@ def test_stepper_graph_replay_equals_eager():
         assert s.learned_steps == 12
         out.append(s.phi_q.cpu().numpy())
     assert np.array_equal(out[0], out[1])
+
+
+def test_spectral_combine_kernel():
+    """amb_learned_spectral_combine against torch complex arithmetic (FP32 rounding)."""
+    torch, L, N = mods()
+    g = torch.Generator(device="cpu").manual_seed(2)
+    H, W = 64, 256
+    shape = (H, W // 2 + 1)
+    rnd = lambda *s_: torch.randn(*s_, generator=g, dtype=torch.complex64).cuda()
+    phi, xi, my, mx, ny_, nx_ = rnd(*shape), rnd(2, *shape), rnd(*shape), rnd(*shape), rnd(*shape), rnd(*shape)
+    # also a transposed (column-major) spectrum, as torch.fft may return, made contiguous by the caller
+    assert torch.fft.rfft2(torch.randn(H, W, device="cuda")).contiguous().is_contiguous()
+    for x_in in (xi, None):
+        out = torch.empty(2, *shape, dtype=torch.complex64, device="cuda")
+        rc = N.lib().amb_learned_spectral_combine(phi.data_ptr(), x_in.data_ptr() if x_in is not None else None,
+                                                  my.data_ptr(), mx.data_ptr(), ny_.data_ptr(), nx_.data_ptr(), 0.7,
+                                                  phi.numel(), out[0].data_ptr(), out[1].data_ptr(),
+                                                  torch.cuda.current_stream().cuda_stream)
+        assert rc == 0, N.last_error()
+        ey, ex = phi * my, phi * mx
+        if x_in is not None:
+            ey, ex = ey + 0.7 * x_in[0] * ny_, ex + 0.7 * x_in[1] * nx_
+        assert float((out[0] - ey).abs().max()) < 1e-5 and float((out[1] - ex).abs().max()) < 1e-5

@@ -124,7 +124,7 @@ def test_face_update_conserves_exactly():
     phi_q = np.rint(rng.uniform(-1, 1, (24, 40)) * OL.FIX).astype(np.int64)
     flux = rng.standard_normal((2, 24, 40)).astype(np.float32)
     xi = rng.standard_normal((2, 24, 40)).astype(np.float32)
-    for kw in ({}, {"xi": xi, "noise_mag": 3.0}):
+    for kw in ({}, {"xi": xi, "noise_mag": 3.0}, {"extra": 0.5 * flux[::-1].copy()}):
         new = OL.face_update(phi_q, flux, 0.05, **kw)
         assert new.sum() == phi_q.sum()
         assert not np.array_equal(new, phi_q)
@@ -186,3 +186,22 @@ def test_linear_part_flux_reproduces_the_k_step_propagator():
     ref = torch.fft.irfft2(torch.fft.rfft2(phi) * a, s=(H, W))
     assert float((new - ref).abs().max()) < 1e-5
     assert abs(float(new.sum() - phi.sum())) < 1e-3
+
+
+def test_spectral_noise_flux_equals_face_sums_of_the_filtered_draw():
+    """LinearPart's noise filters (one spectral pass, as LinearPart.extra combines them on the
+    GPU) equal the order-8 face sums of the noise_filter-shaped draw, component by component."""
+    from activemodelbplus.integrator import Model, Stencil
+    H, W, K = 32, 64, 50
+    st, m = Stencil(1e-3, 1, 1), Model(-0.25, 0, 0.25, 1, 0, 0, 0.05)
+    lin = L.LinearPart((H, W), st, m, K, device="cpu", with_linear=False)
+    xi = torch.from_numpy(np.random.default_rng(4).standard_normal((2, H, W))).float()
+    sxi = torch.fft.rfft2(xi) * 3.0
+    out = torch.stack([torch.fft.irfft2(sxi[0] * lin.ny_, s=(H, W)), torch.fft.irfft2(sxi[1] * lin.nx_, s=(H, W))])
+    g = L.noise_filter((H, W), st, m, K)
+    shaped = torch.fft.irfft2(torch.fft.rfft2(xi) * g, s=(H, W)).numpy().astype(np.float64)
+    w = OL.d8_face_weights()
+    fy = sum(w[i] * np.roll(shaped[0], -e, axis=0) for i, e in enumerate(range(-3, 5))) * 3.0
+    fx = sum(w[i] * np.roll(shaped[1], -e, axis=1) for i, e in enumerate(range(-3, 5))) * 3.0
+    assert np.abs(out[0].numpy() - fy).max() < 1e-4
+    assert np.abs(out[1].numpy() - fx).max() < 1e-4
