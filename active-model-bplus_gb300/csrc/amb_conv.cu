@@ -137,6 +137,23 @@ namespace
         return r < 0 ? r + n : r;
     }
 
+    // Stages the kSites = 132 sites (c0 - 2 .. c0 + 129, periodic in the row) of one channel
+    // chunk of one row into dst as contiguous runs: one bulk copy when the window does not wrap,
+    // at most three when it does (rows of 128 sites wrap on both sides).
+    __device__ __forceinline__ void stage_window(uint8_t* dst, const uint16_t* row_src, int c0, int ncols,
+                                                 uint64_t* bar)
+    {
+        int cur = c0 - 2 < 0 ? c0 - 2 + ncols : c0 - 2;
+        int done = 0;
+        while (done < kSites)
+        {
+            const int len = min(kSites - done, ncols - cur);
+            bulk_g2s(dst + done * 16, row_src + size_t(cur) * 8, uint32_t(len) * 16u, bar);
+            done += len;
+            cur = 0;
+        }
+    }
+
     // GELU in its tanh form (Hendrycks and Gimpel): 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))),
     // with tanh(u) = 1 - 2 / (exp(2u) + 1) (saturates correctly at both ends).
     constexpr float kGeluC0 = 0.7978845608028654f;  // sqrt(2 / pi)
@@ -270,10 +287,14 @@ namespace
     }
 
     // ============================================================== forward
+    // CC = input channel chunks (2 or 4), a compile-time constant so that the MMA issue loop
+    // unrolls and every descriptor is a base plus a constant.
+    template <int CC>
     __global__ void __launch_bounds__(kFwdThreads, 1) conv_fwd_kernel(const FwdArgs a)
     {
         extern __shared__ __align__(1024) uint8_t smem[];
-        const int cc = a.cin_chunks, npad = a.npad, R = a.rows_per_cta;
+        constexpr int cc = CC;
+        const int npad = a.npad, R = a.rows_per_cta;
         const uint32_t wbytes = fwd_weight_bytes(cc, npad);
         const uint32_t slot_bytes = uint32_t(cc) * kRowPlane;
         const uint32_t tcols = fwd_tmem_cols(npad, R);
@@ -328,8 +349,6 @@ namespace
                 // the MMAs consume them
                 mbar_expect_tx(wbar, wbytes);
                 bulk_g2s(wsm, a.wimg, wbytes, wbar);
-                const int cl = (c0 - 2 + a.ncols) % a.ncols;
-                const int cr = (c0 + kTile) % a.ncols;
                 for (int i = 0; i < nin; ++i)
                 {
                     const int row = wrap_row(r0 - 2 + i, a.nrows);
@@ -338,10 +357,7 @@ namespace
                     for (int q = 0; q < cc; ++q)
                     {
                         const uint16_t* src = a.in + (size_t(b * cc + q) * a.nrows + row) * size_t(a.ncols) * 8;
-                        uint8_t* d = dst + q * kRowPlane;
-                        bulk_g2s(d, src + size_t(cl) * 8, 32, &full[i]);
-                        bulk_g2s(d + 32, src + size_t(c0) * 8, kTile * 16, &full[i]);
-                        bulk_g2s(d + 32 + kTile * 16, src + size_t(cr) * 8, 32, &full[i]);
+                        stage_window(dst + q * kRowPlane, src, c0, a.ncols, &full[i]);
                     }
                 }
                 // no copy may still be in flight when the CTA exits
@@ -373,16 +389,18 @@ namespace
                         const int n = npad * (s_hi - s_lo + 1);
                         const uint32_t idesc = idesc_bf16(128, n, false, false);
                         const uint32_t d = tbase + uint32_t((i - 4 + s_lo) * npad);
-                        const uint32_t sa = rsa + i * slot_bytes;
+                        // base descriptors of this row; every MMA adds (byte offset >> 4) to the start
+                        // address field (addresses stay below 256 KiB, so the 14-bit field never carries)
+                        const uint64_t a0 = smem_desc(rsa + i * slot_bytes, kRowPlane, 128);
+                        const uint64_t b0 = smem_desc(wsa + uint32_t(s_lo * npad * 16), kblock, 128);
+                        const uint64_t bstep = kblock >> 4;
+#pragma unroll
                         for (int kx = 0; kx < 5; ++kx)
+#pragma unroll
                             for (int ks = 0; ks < cc / 2; ++ks)
-                            {
-                                const uint64_t ad = smem_desc(sa + 2 * ks * kRowPlane + kx * 16, kRowPlane, 128);
-                                const uint64_t bd = smem_desc(
-                                    wsa + (kx * cc + 2 * ks) * kblock + uint32_t(s_lo * npad * 16), kblock, 128);
-                                mma_bf16(d, ad, bd, idesc, 1u);
-                                issued_any = true;
-                            }
+                                mma_bf16(d, a0 + uint64_t((2 * ks * kRowPlane + kx * 16) >> 4),
+                                         b0 + uint64_t(kx * cc + 2 * ks) * bstep, idesc, 1u);
+                        issued_any = true;
                     }
                     if (i >= 4) mma_commit(&accf[i - 4]);  // output row i - 4 has all five y taps
                 }
@@ -544,18 +562,13 @@ namespace
             {
                 const uint32_t bytes = uint32_t(nx_rows) * xrow + uint32_t(nout) * dzrow;
                 mbar_expect_tx(ld, bytes);
-                const int cl = (c0 - 2 + a.ncols) % a.ncols;
-                const int cr = (c0 + kTile) % a.ncols;
                 for (int i = 0; i < nx_rows; ++i)
                 {
                     const int row = wrap_row(r0 - 2 + i, a.nrows);
                     for (int q = 0; q < cc; ++q)
                     {
                         const uint16_t* src = a.x + (size_t(b * cc + q) * a.nrows + row) * size_t(a.ncols) * 8;
-                        uint8_t* d = xs + i * xrow + q * kRowPlane;
-                        bulk_g2s(d, src + size_t(cl) * 8, 32, ld);
-                        bulk_g2s(d + 32, src + size_t(c0) * 8, kTile * 16, ld);
-                        bulk_g2s(d + 32 + kTile * 16, src + size_t(cr) * 8, 32, ld);
+                        stage_window(xs + i * xrow + q * kRowPlane, src, c0, a.ncols, ld);
                     }
                 }
                 for (int j = 0; j < nout; ++j)
@@ -837,7 +850,7 @@ namespace
     // Raises a kernel's dynamic shared-memory limit once per device (so that later
     // launches, e.g. inside a stream capture, make no attribute calls).
     std::mutex g_attr_mutex;
-    int g_attr_selftest[64], g_attr_fwd[64], g_attr_wgrad[64];
+    int g_attr_selftest[64], g_attr_fwd[64], g_attr_fwd2[64], g_attr_wgrad[64];
 
     cudaError_t set_smem_attr(const void* fn, uint32_t bytes, int (&done)[64])
     {
@@ -922,11 +935,13 @@ extern "C" int amb_conv5x5_forward(const void* in, int batch, int nrows, int nco
     a.rows_per_cta = choose_fwd_rows(batch, nrows, nwin, a.cin_chunks, npad);
     a.error = error;
     const uint32_t smem = fwd_smem_bytes(a.cin_chunks, npad, a.rows_per_cta);
-    cudaError_t e = set_smem_attr(reinterpret_cast<const void*>(conv_fwd_kernel), kSmemLimit, g_attr_fwd);
+    auto kern = a.cin_chunks == 4 ? conv_fwd_kernel<4> : conv_fwd_kernel<2>;
+    cudaError_t e = set_smem_attr(reinterpret_cast<const void*>(kern), kSmemLimit,
+                                  a.cin_chunks == 4 ? g_attr_fwd : g_attr_fwd2);
     if (e == cudaSuccess)
     {
         const long long grid = (long long)batch * nwin * ((nrows + a.rows_per_cta - 1) / a.rows_per_cta);
-        conv_fwd_kernel<<<unsigned(grid), kFwdThreads, smem, static_cast<cudaStream_t>(stream)>>>(a);
+        kern<<<unsigned(grid), kFwdThreads, smem, static_cast<cudaStream_t>(stream)>>>(a);
         e = cudaGetLastError();
     }
     return e == cudaSuccess ? AMB_OK : fail_cuda("amb_conv5x5_forward", e);
