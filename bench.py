@@ -66,6 +66,8 @@ def parse_args():
                     help="learned coarse stepper vs plain FP32: time to --t-end on a 512^2 AMB+ field")
     ap.add_argument("--t-end", type=float, default=1000.0)
     ap.add_argument("--weights", default=os.path.join(PKG, "activemodelbplus", "weights", "fluxnet_k50.npz"))
+    ap.add_argument("--seg-rows", type=int, default=0, help="--launches: sliding-kernel row-segment height")
+    ap.add_argument("--pairs", type=int, default=0, help="--launches: sliding-kernel warp pairs per CTA")
     ap.add_argument("--launches", type=int, default=0,
                     help="profiling driver: run this many bare step launches through the C ABI and exit")
     return ap.parse_args()
@@ -390,7 +392,7 @@ def run_launches(args, w):
                             args.launches, None, stream, None)
     else:
         res = torch.zeros(a.shape, dtype=torch.int16, device="cuda") if args.precision == "f32c" else None
-        cfg = N.amb_kernel_config({"auto": 0, "tile": 1, "sliding": 2}[args.kernel], 0, 0, 0)
+        cfg = N.amb_kernel_config({"auto": 0, "tile": 1, "sliding": 2}[args.kernel], args.seg_rows, args.pairs, 0)
         rc = L.amb_step_f32_ex(ctypes.byref(s), ctypes.byref(m), 1, w["ny"], w["nx"], a.data_ptr(), b.data_ptr(),
                                res.data_ptr() if res is not None else None, 0, args.launches, None, ctypes.byref(cfg),
                                stream, None)
