@@ -66,6 +66,8 @@ def parse_args():
                     help="learned coarse stepper vs plain FP32: time to --t-end on a 512^2 AMB+ field")
     ap.add_argument("--t-end", type=float, default=1000.0)
     ap.add_argument("--weights", default=os.path.join(PKG, "activemodelbplus", "weights", "fluxnet_k50.npz"))
+    ap.add_argument("--learned-launches", type=int, default=0,
+                    help="profiling: N forward passes of the learned stepper's network on a 512^2 field")
     ap.add_argument("--seg-rows", type=int, default=0, help="--launches: sliding-kernel row-segment height")
     ap.add_argument("--pairs", type=int, default=0, help="--launches: sliding-kernel warp pairs per CTA")
     ap.add_argument("--launches", type=int, default=0,
@@ -440,6 +442,23 @@ def run_ensemble(args):
     ens.close()
 
 
+def run_learned_launches(args):
+    """Bare forward passes of the flux network (6 tensor-core convolutions) on one 512^2 field
+    of the learned workload, for profilers."""
+    import torch
+    from activemodelbplus import learned as L
+    net = L.FluxNet.load(args.weights)
+    net.refresh()
+    phi = torch.from_numpy(-0.4 + 0.01 * np.random.default_rng(0).standard_normal((1, 512, 512))).float().cuda()
+    params = torch.tensor([[-4.0, -1.0, 0.05]], device="cuda")
+    x = L.network_input(phi, params)
+    for _ in range(args.learned_launches):
+        flux = net.forward(x)
+    torch.cuda.synchronize()
+    net.check_error()
+    print(json.dumps({"learned_launches": args.learned_launches, "flux_rms": float(flux.square().mean().sqrt())}))
+
+
 def run_learned(args):
     """Learned coarse stepper (K = 50 Euler steps per network evaluation) against the plain
     FP32 integrator, both from the same seeded 512^2 field (phi = -0.4 + 0.01 N(0,1), numpy seed
@@ -481,6 +500,8 @@ def main():
         return run_ensemble(args)
     if args.learned:
         return run_learned(args)
+    if args.learned_launches > 0:
+        return run_learned_launches(args)
     if args.impl == "reference":
         return run_reference_arm(args, w, rank, world)
     import torch
