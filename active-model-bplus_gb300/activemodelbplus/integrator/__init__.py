@@ -182,10 +182,12 @@ class Integrator:
             the fastest; otherwise a shape heuristic decides. The two FP32 kernels agree
             to FP32 rounding, not bitwise; name a kernel for bitwise reproducibility
             across processes.
+        launch: explicit launch shape of the sliding kernel, {"seg_rows": h, "pairs_per_cta": p}
+            (FP32 storage with kernel="sliding"; e.g. a configuration the autotuner reported).
     """
 
     def __init__(self, field, stencil, model, *, precision: str = "f64", seed: int | None = None,
-                 device=None, kernel: str = "auto", autotune: bool = True):
+                 device=None, kernel: str = "auto", autotune: bool = True, launch: dict | None = None):
         torch = _torch()
         if not torch.cuda.is_available():
             raise CudaException("no CUDA device is available")
@@ -221,6 +223,12 @@ class Integrator:
         self._s = N.stencil_struct(self._stencil)
         self._m = N.model_struct(self._model)
         self.set_field(host)
+        self._launch_cfg = None
+        if launch is not None:
+            if precision == "f64" or kernel != "sliding":
+                raise ValueError('launch= applies to FP32 storage with kernel="sliding"')
+            self._launch_cfg = N.amb_kernel_config(N.AMB_KERNEL_SLIDING, int(launch.get("seg_rows", 0)),
+                                                   int(launch.get("pairs_per_cta", 0)), 0)
         self._tuned = None
         if autotune and kernel == "auto" and precision != "f64":
             cfg, us = N.amb_kernel_config(), ctypes.c_double()
@@ -305,9 +313,14 @@ class Integrator:
                                       ctypes.byref(in_spare))
             else:
                 res = self._residual.data_ptr() if self._residual is not None else None
-                rc = lib.amb_step_f32(ctypes.byref(self._s), ctypes.byref(self._m), self._seed, self._ny, self._nx,
-                                      cur.data_ptr(), other.data_ptr(), res, self._timestep, nsteps, None,
-                                      _KERNELS[self._kernel], stream, ctypes.byref(in_spare))
+                if self._launch_cfg is not None:
+                    rc = lib.amb_step_f32_ex(ctypes.byref(self._s), ctypes.byref(self._m), self._seed, self._ny,
+                                             self._nx, cur.data_ptr(), other.data_ptr(), res, self._timestep, nsteps,
+                                             None, ctypes.byref(self._launch_cfg), stream, ctypes.byref(in_spare))
+                else:
+                    rc = lib.amb_step_f32(ctypes.byref(self._s), ctypes.byref(self._m), self._seed, self._ny,
+                                          self._nx, cur.data_ptr(), other.data_ptr(), res, self._timestep, nsteps,
+                                          None, _KERNELS[self._kernel], stream, ctypes.byref(in_spare))
             if self._events is not None:
                 self._events[1].record()
             _check(rc)

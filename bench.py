@@ -66,10 +66,13 @@ def parse_args():
                     help="learned coarse stepper vs plain FP32: time to --t-end on a 512^2 AMB+ field")
     ap.add_argument("--t-end", type=float, default=1000.0)
     ap.add_argument("--weights", default=os.path.join(PKG, "activemodelbplus", "weights", "fluxnet_k50.npz"))
+    ap.add_argument("--learned-steps", type=int, default=0,
+                    help="time N macro steps of the learned stepper on the 512^2 field (after 40 untimed)")
     ap.add_argument("--learned-launches", type=int, default=0,
                     help="profiling: N forward passes of the learned stepper's network on a 512^2 field")
-    ap.add_argument("--seg-rows", type=int, default=0, help="--launches: sliding-kernel row-segment height")
-    ap.add_argument("--pairs", type=int, default=0, help="--launches: sliding-kernel warp pairs per CTA")
+    ap.add_argument("--seg-rows", type=int, default=0,
+                    help="with --kernel sliding: row-segment height (e.g. the autotuner's choice, for profiling)")
+    ap.add_argument("--pairs", type=int, default=0, help="with --kernel sliding: warp pairs per CTA")
     ap.add_argument("--launches", type=int, default=0,
                     help="profiling driver: run this many bare step launches through the C ABI and exit")
     return ap.parse_args()
@@ -279,7 +282,10 @@ def run_ours(args, w, rank, world, dist):
     model = Model(w["a"], w["b"], w["c"], w["kappa"], w["lamb"], w["zeta"], w["T"])
     field = initial_field(w, rank)
     sites = w["ny"] * w["nx"]
-    sim = Integrator(field, stencil, model, precision=args.precision, seed=1000 + rank, kernel=args.kernel)
+    launch = ({"seg_rows": args.seg_rows, "pairs_per_cta": args.pairs}
+              if args.kernel == "sliding" and (args.seg_rows or args.pairs) else None)
+    sim = Integrator(field, stencil, model, precision=args.precision, seed=1000 + rank, kernel=args.kernel,
+                     launch=launch)
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
 
     def barrier():
@@ -361,7 +367,7 @@ def run_ours(args, w, rank, world, dist):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "f64" else "f32", "data": "synthetic",
-        "config": dict(config_of(args, w), kernel_config=sim.kernel_config),
+        "config": dict(config_of(args, w), kernel_config=sim.kernel_config or launch),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s", "traffic": measured_traffic(args),
@@ -459,6 +465,27 @@ def run_learned_launches(args):
     print(json.dumps({"learned_launches": args.learned_launches, "flux_rms": float(flux.square().mean().sqrt())}))
 
 
+def run_learned_steps(args):
+    """N macro steps (K = 50 Euler steps each) of the learned stepper on the 512^2 field of the
+    learned workload, after 40 untimed ones (graph capture, first checks); wall time per macro
+    step, CUDA-synchronised, including its residual checks (one per 20 macro steps)."""
+    import torch
+    from activemodelbplus import learned as L
+    from activemodelbplus.integrator import Model, Stencil
+    net = L.FluxNet.load(args.weights)
+    field = -0.4 + 0.01 * np.random.default_rng(0).standard_normal((512, 512))
+    st = L.LearnedStepper(net, field, Stencil(1e-3, 1, 1), Model(-0.25, 0, 0.25, 1, -1, -4, 0.05), K=net.K,
+                          check_every=20, tol=0.5, residual_sigma=2.0)
+    st.advance(40)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st.advance(args.learned_steps)
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    print(json.dumps({"learned_macro_steps": args.learned_steps, "us_per_macro_step": 1e6 * sec / args.learned_steps,
+                      "euler_steps_per_macro_step": net.K, "fallback_spans": st.fallback_spans}))
+
+
 def run_learned(args):
     """Learned coarse stepper (K = 50 Euler steps per network evaluation) against the plain
     FP32 integrator, both from the same seeded 512^2 field (phi = -0.4 + 0.01 N(0,1), numpy seed
@@ -502,6 +529,8 @@ def main():
         return run_learned(args)
     if args.learned_launches > 0:
         return run_learned_launches(args)
+    if args.learned_steps > 0:
+        return run_learned_steps(args)
     if args.impl == "reference":
         return run_reference_arm(args, w, rank, world)
     import torch

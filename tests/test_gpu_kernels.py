@@ -153,3 +153,16 @@ def test_autotuner_choice_is_used_and_cached():
     auto = run_f32(field, p, 10, kernel=0)
     explicit = run_f32(field, p, 10, kernel=cfg.kernel, seg_rows=cfg.seg_rows, pairs=cfg.pairs_per_cta)
     assert np.array_equal(auto, explicit)
+
+
+def test_integrator_explicit_launch_shape():
+    """Integrator(kernel="sliding", launch=...) runs the given launch shape: bitwise equal to the
+    device-pointer call with the same configuration."""
+    from activemodelbplus.integrator import Integrator, Model, Stencil
+    p = Params(T=0.05, **AMB)
+    field = initial((96, 448), seed=13)
+    sim = Integrator(field, Stencil(p.dt, p.dx, p.dy), Model(p.a, p.b, p.c, p.kappa, p.lamb, p.zeta, p.T),
+                     precision="f32", seed=7, kernel="sliding", launch={"seg_rows": 16, "pairs_per_cta": 4})
+    sim.run(10)
+    ref = run_f32(field, p, 10, kernel=2, seg_rows=16, pairs=4, comp=False, seed=7)
+    assert np.array_equal(sim.field, ref)
