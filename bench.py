@@ -47,7 +47,7 @@ UNIT = "Gsite-updates/s"
 BYTES_PER_SITE = 8  # algorithmic: read phi (4 B) + write phi (4 B), FP32 path
 
 
-def parse_args():
+def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -75,7 +75,7 @@ def parse_args():
     ap.add_argument("--pairs", type=int, default=0, help="with --kernel sliding: warp pairs per CTA")
     ap.add_argument("--launches", type=int, default=0,
                     help="profiling driver: run this many bare step launches through the C ABI and exit")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def workload(args):
@@ -273,6 +273,22 @@ def run_reference_arm(args, w, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(dist, values, device):
+    """Element-wise maximum of per-rank timings across the process group (identity without one)."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
+def job_throughput(world: int, steps: int, inner: int, sites: int, seconds: float) -> float:
+    """Whole-job Gsite-updates/s: every rank advances its own replica (weak scaling), the
+    slowest rank's time counts."""
+    return world * steps * inner * sites / seconds / 1e9
+
+
 def run_ours(args, w, rank, world, dist):
     import torch
     from activemodelbplus.integrator import Integrator, Model, Stencil, _native as N
@@ -314,11 +330,8 @@ def run_ours(args, w, rank, world, dist):
         barrier()
     total_ms = sum(step_ms)
     launch_ms = sum(kern_ms) / (args.steps * args.inner)
-    if dist is not None:
-        t = torch.tensor([total_ms, launch_ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, launch_ms = float(t[0]), float(t[1])
-    value = world * args.steps * args.inner * sites / (total_ms / 1e3) / 1e9
+    total_ms, launch_ms = max_over_ranks(dist, [total_ms, launch_ms], dev)
+    value = job_throughput(world, args.steps, args.inner, sites, total_ms / 1e3)
 
     # e2e through the C handle with pinned float64 host buffers
     e2e = None
@@ -349,11 +362,8 @@ def run_ours(args, w, rank, world, dist):
                 t0 = time.perf_counter()
                 e2e_step()
                 wall += time.perf_counter() - t0
-            if dist is not None:
-                t = torch.tensor([wall], dtype=torch.float64, device=dev)
-                dist.all_reduce(t, op=dist.ReduceOp.MAX)
-                wall = float(t[0])
-            e2e = {"value": world * args.steps * args.inner * sites / wall / 1e9, "unit": UNIT,
+            wall = max_over_ranks(dist, [wall], dev)[0]
+            e2e = {"value": job_throughput(world, args.steps, args.inner, sites, wall), "unit": UNIT,
                    "h2d_bytes_per_step": int(host_in.numel() * 8), "d2h_bytes_per_step": int(host_out.numel() * 8)}
         finally:
             L.amb_integrator_destroy(h)
