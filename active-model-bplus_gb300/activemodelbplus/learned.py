@@ -514,6 +514,8 @@ class LinearPart:
         self.mx = torch.from_numpy(np.broadcast_to(mx, full).astype(np.complex64)).to(dev)
         self.ny_ = torch.from_numpy(np.broadcast_to(g * sym_y, full).astype(np.complex64)).to(dev)
         self.nx_ = torch.from_numpy(np.broadcast_to(g * sym_x, full).astype(np.complex64)).to(dev)
+        self._layout = None
+        self._filters = None
 
     def flux(self, phi):
         """Linear part only: phi [B, H, W] -> G [B, 2, H, W] (component 0 = y face, 1 = x face)."""
@@ -527,16 +529,30 @@ class LinearPart:
         """Linear part of phi [H, W] plus the noise flux of xi [2, H, W] (or None) into out [2, H, W]:
         forward FFTs, one combining kernel (``amb_learned_spectral_combine``), two inverse FFTs."""
         torch = _torch()
-        # cuFFT through torch may return the spectrum in a transposed (column-major) layout;
-        # the combining kernel reads row-major arrays
-        spec = torch.fft.rfft2(phi).contiguous()
-        sxi = torch.fft.rfft2(xi).contiguous() if xi is not None else None
+        spec = torch.fft.rfft2(phi)
+        sxi = torch.fft.rfft2(xi) if xi is not None else None
         if not spec.is_cuda:
             raise CudaException("LinearPart.extra runs on the GPU")
-        comb = torch.empty((2,) + tuple(spec.shape), dtype=spec.dtype, device=spec.device)
+        # cuFFT through torch may return the spectrum in a transposed (column-major) layout: the
+        # combining kernel works in memory order, so the filters are kept in the FFT's layout
+        # (converted once) and the spectra are used as they come when they are dense in it
+        layout = tuple(spec.stride())
+        if self._layout != layout:
+            self._filters = [torch.empty_strided(spec.shape, layout, dtype=spec.dtype, device=spec.device).copy_(f)
+                             for f in (self.my, self.mx, self.ny_, self.nx_)]
+            self._layout = layout
+        n = spec.numel()
+        dense = sum((d - 1) * st for d, st in zip(spec.shape, layout)) + 1 == n and min(layout) >= 1
+        if not dense or (sxi is not None and (tuple(sxi.stride()[1:]) != layout or sxi.stride(0) != n)):
+            spec = torch.empty_strided(spec.shape, layout, dtype=spec.dtype, device=spec.device).copy_(spec)
+            if sxi is not None:
+                sx2 = torch.empty_strided(sxi.shape, (n,) + layout, dtype=sxi.dtype, device=sxi.device)
+                sxi = sx2.copy_(sxi)
+        comb = torch.empty_strided((2,) + tuple(spec.shape), (n,) + layout, dtype=spec.dtype, device=spec.device)
+        my, mx, ny_, nx_ = self._filters
         _check(N.lib().amb_learned_spectral_combine(
-            _ptr(spec), _ptr(sxi), _ptr(self.my), _ptr(self.mx), _ptr(self.ny_), _ptr(self.nx_),
-            float(noise_mag), spec.numel(), _ptr(comb[0]), _ptr(comb[1]), _stream()))
+            _ptr(spec), _ptr(sxi), _ptr(my), _ptr(mx), _ptr(ny_), _ptr(nx_),
+            float(noise_mag), n, _ptr(comb[0]), _ptr(comb[1]), _stream()))
         torch.fft.irfft2(comb[0], s=self.shape, out=out[0])
         torch.fft.irfft2(comb[1], s=self.shape, out=out[1])
         return out
@@ -641,8 +657,8 @@ class LearnedStepper:
             self._linear.extra(self.phi_f, self.xi if noisy else None, mag, self._extra)
         _check(lib.amb_learned_update(_ptr(net_flux), _ptr(self._extra), ny, nx, self.dtk, self.stencil.dx,
                                       self.stencil.dy, _ptr(xi_direct), mag if xi_direct is not None else 0.0,
-                                      _ptr(self.phi_q), _ptr(self.phi_f), self.bound, _ptr(self.flag), _stream()))
-        self.step_dev.add_(1)
+                                      _ptr(self.phi_q), _ptr(self.phi_f), self.bound, _ptr(self.flag),
+                                      _ptr(self.step_dev), _stream()))
 
     def _macro_step(self) -> None:
         """One learned macro step (network, noise, fixed-point update, step counter).

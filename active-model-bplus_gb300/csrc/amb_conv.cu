@@ -751,8 +751,11 @@ namespace
     __global__ void learned_update_kernel(const float* __restrict__ flux, const float* __restrict__ extra,
                                           const float* __restrict__ xi, int nrows, int ncols, float scale_y,
                                           float scale_x, float noise_mag, int32_t* __restrict__ phi_q,
-                                          float* __restrict__ phi_f, long long bound, int* __restrict__ flag)
+                                          float* __restrict__ phi_f, long long bound, int* __restrict__ flag,
+                                          int64_t* __restrict__ advance)
     {
+        // the next macro step's noise key (nothing in this launch reads it)
+        if (advance && blockIdx.x == 0 && threadIdx.x == 0) *advance += 1;
         const size_t plane = size_t(nrows) * ncols;
         const float* fy = flux;
         const float* fx = flux + plane;
@@ -1022,7 +1025,7 @@ extern "C" int amb_learned_noise(int nrows, int ncols, uint64_t seed, const int6
 
 extern "C" int amb_learned_update(const float* flux, const float* extra, int nrows, int ncols, double dt_macro,
                                   double dx, double dy, const float* xi, double noise_mag, int32_t* phi_q,
-                                  float* phi_f, double bound, int* flag, void* stream)
+                                  float* phi_f, double bound, int* flag, int64_t* step_to_advance, void* stream)
 {
     if (!flux || !phi_q || !phi_f || !flag || nrows < 1 || ncols < 1 || !(dt_macro > 0) || !(dx > 0) ||
         !(dy > 0) || !(noise_mag >= 0) || !(bound > 0))
@@ -1035,7 +1038,8 @@ extern "C" int amb_learned_update(const float* flux, const float* extra, int nro
     const bool noisy = xi && noise_mag > 0;
     learned_update_kernel<<<grid, 256, 0, s>>>(flux, extra, noisy ? xi : nullptr, nrows, ncols,
                                                float(dt_macro / dy * fix), float(dt_macro / dx * fix),
-                                               noisy ? float(noise_mag) : 0.f, phi_q, phi_f, (long long)qb, flag);
+                                               noisy ? float(noise_mag) : 0.f, phi_q, phi_f, (long long)qb, flag,
+                                               step_to_advance);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_update", e);
 }

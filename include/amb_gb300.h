@@ -298,14 +298,18 @@ int amb_learned_noise(int nrows, int ncols, uint64_t seed, const int64_t* step, 
  * from amb_learned_noise). Face values are formed in FP32 with explicitly rounded operations,
  * scaled by dt_macro/d * 2^24 and rounded to an integer once; each face increment is applied
  * with opposite signs to its two sites, so sum(phi_q) is conserved exactly. phi_f receives
- * phi_q * 2^-24. *flag |= 1 if a flux is non-finite or |phi| exceeds bound (then clamped). */
+ * phi_q * 2^-24. *flag |= 1 if a flux is non-finite or |phi| exceeds bound (then clamped).
+ * step_to_advance (device int64, may be NULL) is incremented once, for the next macro step's
+ * noise key. */
 int amb_learned_update(const float* flux, const float* extra, int nrows, int ncols, double dt_macro, double dx,
                        double dy, const float* xi, double noise_mag, int32_t* phi_q, float* phi_f, double bound,
-                       int* flag, void* stream);
+                       int* flag, int64_t* step_to_advance, void* stream);
 
 /* Spectral step of the learned stepper's linear part and noise: for n complex rfft2 modes
  * (complex64 arrays), out_y = phi_hat * my + noise_mag * xi_hat_y * ny and
- * out_x = phi_hat * mx + noise_mag * xi_hat_x * nx, xi_hat = [2][n] (y then x) or NULL. */
+ * out_x = phi_hat * mx + noise_mag * xi_hat_x * nx, xi_hat = [2][n] (y then x) or NULL.
+ * Element-wise in memory order: all arrays must share one dense layout (of any dimension
+ * order), e.g. the layout the FFT produced. */
 int amb_learned_spectral_combine(const void* phi_hat, const void* xi_hat, const void* my, const void* mx,
                                  const void* ny, const void* nx, double noise_mag, int64_t n, void* out_y,
                                  void* out_x, void* stream);

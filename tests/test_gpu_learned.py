@@ -235,7 +235,7 @@ def test_update_is_exact_and_conservative(T, with_extra):
         assert lib.amb_learned_noise(H, W, 99, step.data_ptr(), xi.data_ptr(), strm) == 0, N.last_error()
     rc = lib.amb_learned_update(flux_dev.data_ptr(), extra_dev.data_ptr() if with_extra else None, H, W, dtk, 1.0,
                                 1.0, xi.data_ptr() if T > 0 else None, mag, q.data_ptr(), f.data_ptr(), 3.0,
-                                flag.data_ptr(), strm)
+                                flag.data_ptr(), step.data_ptr(), strm)
     assert rc == 0, N.last_error()
     got = q.cpu().numpy().astype(np.int64)
     if T > 0:
@@ -249,6 +249,7 @@ def test_update_is_exact_and_conservative(T, with_extra):
     assert got.sum() == phi_q.astype(np.int64).sum()
     assert np.array_equal(f.cpu().numpy(), (got / OL.FIX).astype(np.float32))
     assert int(flag.item()) == 0
+    assert int(step.item()) == 8  # the next macro step's noise key
 
 
 # ------------------------------------------------------------ stepper and training gain
