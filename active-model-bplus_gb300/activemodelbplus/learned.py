@@ -579,7 +579,7 @@ class LearnedStepper:
             are summed undamped, which overstates the high-wavenumber noise.
     """
 
-    def __init__(self, net: FluxNet, field, stencil, model, *, K: int = 50, seed: int = 0, check_every: int = 20,
+    def __init__(self, net: FluxNet, field, stencil, model, *, K: int = 50, seed: int = 0, check_every: int = 40,
                  tol: float = 0.5, bound: float = 3.0, plain_precision: str = "f32", use_graph: bool = True,
                  filter_noise: bool = True, residual_sigma: float = 0.0, atol: float = 0.0):
         torch = _torch()
@@ -834,7 +834,7 @@ def _timed(fn):
 
 
 def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: int | None = None, seed: int = 0,
-                       check_every: int = 20, tol: float = 0.5, plain_seeds=(1, 2, 3), residual_sigma: float = 2.0,
+                       check_every: int = 40, tol: float = 0.5, plain_seeds=(1, 2, 3), residual_sigma: float = 2.0,
                        filter_noise: bool = True, atol: float = 0.0) -> dict:
     """Time to ``t_end`` and end-state statistics of the learned stepper against the plain
     FP32 integrator (the faster of the Integrator and a one-replica CUDA-graph ensemble)
@@ -917,7 +917,7 @@ def _main(argv=None) -> int:
     c.add_argument("--weights", required=True)
     c.add_argument("--size", type=int, default=512)
     c.add_argument("--t-end", type=float, default=1000.0)
-    c.add_argument("--check-every", type=int, default=20)
+    c.add_argument("--check-every", type=int, default=40)
     c.add_argument("--tol", type=float, default=0.5)
     c.add_argument("--seed", type=int, default=0)
     c.add_argument("--temperature", type=float, default=0.05)

@@ -478,14 +478,14 @@ def run_learned_launches(args):
 def run_learned_steps(args):
     """N macro steps (K = 50 Euler steps each) of the learned stepper on the 512^2 field of the
     learned workload, after 40 untimed ones (graph capture, first checks); wall time per macro
-    step, CUDA-synchronised, including its residual checks (one per 20 macro steps)."""
+    step, CUDA-synchronised, including its residual checks (one per 40 macro steps)."""
     import torch
     from activemodelbplus import learned as L
     from activemodelbplus.integrator import Model, Stencil
     net = L.FluxNet.load(args.weights)
     field = -0.4 + 0.01 * np.random.default_rng(0).standard_normal((512, 512))
     st = L.LearnedStepper(net, field, Stencil(1e-3, 1, 1), Model(-0.25, 0, 0.25, 1, -1, -4, 0.05), K=net.K,
-                          check_every=20, tol=0.5, residual_sigma=2.0)
+                          check_every=40, tol=0.5, residual_sigma=2.0)
     st.advance(40)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
