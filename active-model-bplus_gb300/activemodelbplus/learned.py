@@ -516,6 +516,7 @@ class LinearPart:
         self.nx_ = torch.from_numpy(np.broadcast_to(g * sym_x, full).astype(np.complex64)).to(dev)
         self._layout = None
         self._filters = None
+        self._noise_buf = None
 
     def flux(self, phi):
         """Linear part only: phi [B, H, W] -> G [B, 2, H, W] (component 0 = y face, 1 = x face)."""
@@ -525,9 +526,12 @@ class LinearPart:
         gx = torch.fft.irfft2(spec * self.mx, s=self.shape)
         return torch.stack([gy, gx], dim=1)
 
-    def extra(self, phi, xi, noise_mag: float, out):
+    def extra(self, phi, xi, noise_mag: float, out, spectral_noise=None):
         """Linear part of phi [H, W] plus the noise flux of xi [2, H, W] (or None) into out [2, H, W]:
-        forward FFTs, one combining kernel (``amb_learned_spectral_combine``), two inverse FFTs."""
+        forward FFTs, one combining kernel (``amb_learned_spectral_combine``), two inverse FFTs.
+        ``spectral_noise=(seed, step)`` draws the noise spectrum directly
+        (``amb_learned_noise_spectral``, keyed by the device step counter) instead of
+        transforming xi: statistically the same white noise, two forward FFTs fewer."""
         torch = _torch()
         spec = torch.fft.rfft2(phi)
         sxi = torch.fft.rfft2(xi) if xi is not None else None
@@ -535,19 +539,28 @@ class LinearPart:
             raise CudaException("LinearPart.extra runs on the GPU")
         # cuFFT through torch may return the spectrum in a transposed (column-major) layout: the
         # combining kernel works in memory order, so the filters are kept in the FFT's layout
-        # (converted once) and the spectra are used as they come when they are dense in it
+        # (converted once) and the spectra are used as they come when they are dense in it; a
+        # drawn noise spectrum is written straight into that layout
         layout = tuple(spec.stride())
+        n = spec.numel()
+        if sum((d - 1) * st for d, st in zip(spec.shape, layout)) + 1 != n or min(layout) < 1:
+            layout = (spec.shape[1], 1)   # not dense in its own strides: work row-major
         if self._layout != layout:
             self._filters = [torch.empty_strided(spec.shape, layout, dtype=spec.dtype, device=spec.device).copy_(f)
                              for f in (self.my, self.mx, self.ny_, self.nx_)]
             self._layout = layout
-        n = spec.numel()
-        dense = sum((d - 1) * st for d, st in zip(spec.shape, layout)) + 1 == n and min(layout) >= 1
-        if not dense or (sxi is not None and (tuple(sxi.stride()[1:]) != layout or sxi.stride(0) != n)):
+        if spectral_noise is not None:
+            if self._noise_buf is None or tuple(self._noise_buf.stride()) != (n,) + layout:
+                self._noise_buf = torch.empty_strided((2,) + tuple(spec.shape), (n,) + layout, dtype=spec.dtype,
+                                                      device=spec.device)
+            seed, step = spectral_noise
+            _check(N.lib().amb_learned_noise_spectral(self.shape[0], self.shape[1], int(seed), _ptr(step),
+                                                      _ptr(self._noise_buf), layout[0], layout[1], _stream()))
+            sxi = self._noise_buf
+        if tuple(spec.stride()) != layout:
             spec = torch.empty_strided(spec.shape, layout, dtype=spec.dtype, device=spec.device).copy_(spec)
-            if sxi is not None:
-                sx2 = torch.empty_strided(sxi.shape, (n,) + layout, dtype=sxi.dtype, device=sxi.device)
-                sxi = sx2.copy_(sxi)
+        if sxi is not None and (tuple(sxi.stride()[1:]) != layout or sxi.stride(0) != n):
+            sxi = torch.empty_strided(sxi.shape, (n,) + layout, dtype=sxi.dtype, device=sxi.device).copy_(sxi)
         comb = torch.empty_strided((2,) + tuple(spec.shape), (n,) + layout, dtype=spec.dtype, device=spec.device)
         my, mx, ny_, nx_ = self._filters
         _check(N.lib().amb_learned_spectral_combine(
@@ -577,11 +590,15 @@ class LearnedStepper:
         filter_noise: shape the K-step noise draw with :func:`noise_filter` (the K-step
             accumulation of the linearised plain scheme); without it the K one-step draws
             are summed undamped, which overstates the high-wavenumber noise.
+        spectral_noise: with ``filter_noise``, draw the noise spectrum directly
+            (``amb_learned_noise_spectral``) instead of drawing two normals per site and
+            transforming them; the same distribution, two forward FFTs fewer per macro step.
     """
 
     def __init__(self, net: FluxNet, field, stencil, model, *, K: int = 50, seed: int = 0, check_every: int = 40,
                  tol: float = 0.5, bound: float = 3.0, plain_precision: str = "f32", use_graph: bool = True,
-                 filter_noise: bool = True, residual_sigma: float = 0.0, atol: float = 0.0):
+                 filter_noise: bool = True, residual_sigma: float = 0.0, atol: float = 0.0,
+                 spectral_noise: bool = True):
         torch = _torch()
         self.net = net
         self.stencil = Stencil(stencil)
@@ -593,6 +610,7 @@ class LearnedStepper:
         self.tol = float(tol)
         self.bound = float(bound)
         self.atol = float(atol)
+        self.spectral_noise = bool(spectral_noise)
         host = np.asarray(field, dtype=np.float64)
         self.shape = host.shape
         dev = torch.device("cuda")
@@ -645,16 +663,21 @@ class LearnedStepper:
         ny, nx = self.shape
         net_flux = self.net.forward(network_input(self.phi_f.unsqueeze(0), self.params))
         noisy = noisy and self.model.T > 0
-        if noisy:
-            _check(lib.amb_learned_noise(ny, nx, self.seed, _ptr(self.step_dev), _ptr(self.xi), _stream()))
         mag = math.sqrt(2.0 * self.model.T) * math.sqrt(1.0 / (self.dtk * self.stencil.dx * self.stencil.dy))
         xi_direct = None
         if self._g is None and noisy:
             # unfiltered noise: the update kernel forms the face sums of xi itself
+            _check(lib.amb_learned_noise(ny, nx, self.seed, _ptr(self.step_dev), _ptr(self.xi), _stream()))
             self._linear.extra(self.phi_f, None, 0.0, self._extra)
             xi_direct = self.xi
+        elif noisy and self.spectral_noise:
+            # filtered noise drawn directly as a spectrum, shaped and added in the spectral pass
+            self._linear.extra(self.phi_f, None, mag, self._extra, spectral_noise=(self.seed, self.step_dev))
+        elif noisy:
+            _check(lib.amb_learned_noise(ny, nx, self.seed, _ptr(self.step_dev), _ptr(self.xi), _stream()))
+            self._linear.extra(self.phi_f, self.xi, mag, self._extra)
         else:
-            self._linear.extra(self.phi_f, self.xi if noisy else None, mag, self._extra)
+            self._linear.extra(self.phi_f, None, 0.0, self._extra)
         _check(lib.amb_learned_update(_ptr(net_flux), _ptr(self._extra), ny, nx, self.dtk, self.stencil.dx,
                                       self.stencil.dy, _ptr(xi_direct), mag if xi_direct is not None else 0.0,
                                       _ptr(self.phi_q), _ptr(self.phi_f), self.bound, _ptr(self.flag),
@@ -835,12 +858,13 @@ def _timed(fn):
 
 def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: int | None = None, seed: int = 0,
                        check_every: int = 40, tol: float = 0.5, plain_seeds=(1, 2, 3), residual_sigma: float = 2.0,
-                       filter_noise: bool = True, atol: float = 0.0) -> dict:
+                       filter_noise: bool = True, atol: float = 0.0, learned_runs: int = 3) -> dict:
     """Time to ``t_end`` and end-state statistics of the learned stepper against the plain
     FP32 integrator (the faster of the Integrator and a one-replica CUDA-graph ensemble)
     from the same initial field: S(k) mean wavenumber (the reference notebook's
-    definition), droplet count, mass. The plain run is repeated with ``plain_seeds`` to
-    show the spread of its statistics."""
+    definition), droplet count, mass. The plain run is repeated with ``plain_seeds`` and the
+    learned run with ``learned_runs`` noise seeds (``seed``, ``seed + 1``, ...): the error is
+    that of the learned mean against the plain mean, the speed-up that of the fastest runs."""
     from .analysis import count_droplets, mean_wavenumber, structure_factor
     stencil, model = Stencil(stencil), Model(model)
     K = int(K if K is not None else getattr(net, "K", 50))
@@ -875,23 +899,37 @@ def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: 
         res["plain"].append({"seconds": sec, "seed": sd, "k_avg": mean_wavenumber(k, S),
                              "k_peak": float(k[np.nanargmax(S)]), "droplets": count_droplets(f, phi0),
                              "mass_drift": float(f.sum() - field.sum())})
-    st = LearnedStepper(net, field, stencil, model, K=K, seed=seed, check_every=check_every, tol=tol,
-                        residual_sigma=residual_sigma, filter_noise=filter_noise, atol=atol)
-    m0 = st.mass_q()
-    sec = _timed(lambda: st.run_for_time(t_end))
-    f = st.field
-    k, S, _ = structure_factor(f, stencil.dx, stencil.dy, phi0=phi0)
-    res["learned"] = {"seconds": sec, "k_avg": mean_wavenumber(k, S), "k_peak": float(k[np.nanargmax(S)]),
-                      "droplets": count_droplets(f, phi0), "mass_q_drift": st.mass_q() - m0,
-                      "macro_steps": st.macro_steps, "learned_macro_steps": st.learned_steps,
-                      "fallback_spans": st.fallback_spans,
-                      "median_residual": float(np.median(st.residuals)) if st.residuals else None}
+    res["learned_runs"] = []
+    for sd in range(seed, seed + max(1, int(learned_runs))):
+        st = LearnedStepper(net, field, stencil, model, K=K, seed=sd, check_every=check_every, tol=tol,
+                            residual_sigma=residual_sigma, filter_noise=filter_noise, atol=atol)
+        m0 = st.mass_q()
+        sec = _timed(lambda: st.run_for_time(t_end))
+        f = st.field
+        k, S, _ = structure_factor(f, stencil.dx, stencil.dy, phi0=phi0)
+        res["learned_runs"].append({"seconds": sec, "seed": sd, "k_avg": mean_wavenumber(k, S),
+                                    "k_peak": float(k[np.nanargmax(S)]), "droplets": count_droplets(f, phi0),
+                                    "mass_q_drift": st.mass_q() - m0, "macro_steps": st.macro_steps,
+                                    "learned_macro_steps": st.learned_steps, "fallback_spans": st.fallback_spans,
+                                    "median_residual": float(np.median(st.residuals)) if st.residuals else None})
+        del st
+    runs = res["learned_runs"]
+    res["learned"] = runs[0]
     plain_k = np.array([p["k_avg"] for p in res["plain"]])
+    learned_k = np.array([r["k_avg"] for r in runs])
     res["plain_k_avg_mean"] = float(plain_k.mean())
     res["plain_k_avg_std"] = float(plain_k.std())
-    res["k_avg_rel_err"] = abs(res["learned"]["k_avg"] - plain_k.mean()) / plain_k.mean()
+    res["learned_k_avg_mean"] = float(learned_k.mean())
+    res["learned_k_avg_std"] = float(learned_k.std())
+    res["k_avg_rel_err"] = abs(learned_k.mean() - plain_k.mean()) / plain_k.mean()
+    # standard error of that difference of means (sample standard deviations)
+    se2 = sum(float(v.std(ddof=1)) ** 2 / len(v) for v in (plain_k, learned_k) if len(v) > 1)
+    res["k_avg_rel_err_se"] = float(np.sqrt(se2)) / float(plain_k.mean())
     res["plain_seconds_min"] = float(min(p["seconds"] for p in res["plain"]))
-    res["speedup"] = res["plain_seconds_min"] / sec
+    res["learned_seconds_min"] = float(min(r["seconds"] for r in runs))
+    res["learned_fallback_spans"] = int(sum(r["fallback_spans"] for r in runs))
+    res["learned_mass_q_drift_max"] = int(max(abs(r["mass_q_drift"]) for r in runs))
+    res["speedup"] = res["plain_seconds_min"] / res["learned_seconds_min"]
     return res
 
 

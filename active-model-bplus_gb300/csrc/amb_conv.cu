@@ -155,25 +155,28 @@ namespace
     }
 
     // GELU in its tanh form (Hendrycks and Gimpel): 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))),
-    // with tanh(u) = 1 - 2 / (exp(2u) + 1) (saturates correctly at both ends).
+    // with the hardware tanh approximation (relative error about 2^-11, below the bf16 rounding
+    // of the stored activations; end-state statistics of long learned runs are unchanged by it).
     constexpr float kGeluC0 = 0.7978845608028654f;  // sqrt(2 / pi)
     constexpr float kGeluC1 = 0.044715f;
 
-    __device__ __forceinline__ float tanh_via_exp(float u)
+    __device__ __forceinline__ float tanh_hw(float u)
     {
-        return 1.f - __fdividef(2.f, __expf(2.f * u) + 1.f);
+        float t;
+        asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+        return t;
     }
 
     __device__ __forceinline__ float gelu_f(float z)
     {
-        const float t = tanh_via_exp(kGeluC0 * z * (1.f + kGeluC1 * z * z));
+        const float t = tanh_hw(kGeluC0 * z * (1.f + kGeluC1 * z * z));
         return 0.5f * z * (1.f + t);
     }
 
     __device__ __forceinline__ float gelu_grad_f(float z)
     {
         const float z2 = z * z;
-        const float t = tanh_via_exp(kGeluC0 * z * (1.f + kGeluC1 * z2));
+        const float t = tanh_hw(kGeluC0 * z * (1.f + kGeluC1 * z2));
         return 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * kGeluC0 * (1.f + 3.f * kGeluC1 * z2);
     }
 
@@ -705,6 +708,53 @@ namespace
         }
     }
 
+    // The rfft2 spectra of two real white-noise fields of unit variance per site, drawn directly:
+    // out[comp][r][k] at out + comp * n + r * rs + k * ks (complex64; k < ncols/2 + 1). Off the
+    // self-conjugate columns (k = 0 and, for even ncols, k = ncols/2) each mode is a complex
+    // normal with E|z|^2 = nrows ncols; in those columns mode r is the conjugate of mode
+    // nrows - r, and the self-conjugate modes (r = 0, r = nrows/2) are real with the same
+    // variance. One Philox call per (r, k) (keyed by the lower of r and nrows - r in those
+    // columns) gives both components.
+    __global__ void learned_noise_spectral_kernel(float2* __restrict__ out, int nrows, int ncols, int64_t rs,
+                                                  int64_t ks, int64_t n, uint64_t seed,
+                                                  const int64_t* __restrict__ step)
+    {
+        const int nk = ncols / 2 + 1;
+        const int64_t st = *step;
+        const float s_half = sqrtf(0.5f * float(nrows) * float(ncols));
+        const float s_full = sqrtf(float(nrows) * float(ncols));
+        const int64_t total = int64_t(nrows) * nk;
+        for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total;
+             i += int64_t(gridDim.x) * blockDim.x)
+        {
+            const int r = int(i / nk), k = int(i - int64_t(r) * nk);
+            const bool herm = k == 0 || (ncols % 2 == 0 && k == ncols / 2);
+            int rr = r;
+            bool conj = false;
+            if (herm && r > nrows / 2)
+            {
+                rr = nrows - r;
+                conj = true;
+            }
+            const amb::U4 b = amb::noise_bits(seed, st, rr, 4 * k, 0);
+            const float2 z0 = amb::box_muller_f32(b.x, b.y), z1 = amb::box_muller_f32(b.z, b.w);
+            float2 vy = make_float2(z0.x * s_half, z0.y * s_half);
+            float2 vx = make_float2(z1.x * s_half, z1.y * s_half);
+            if (herm && (rr == 0 || (nrows % 2 == 0 && rr == nrows / 2)))
+            {
+                vy = make_float2(z0.x * s_full, 0.f);
+                vx = make_float2(z1.x * s_full, 0.f);
+            }
+            if (conj)
+            {
+                vy.y = -vy.y;
+                vx.y = -vx.y;
+            }
+            out[int64_t(r) * rs + int64_t(k) * ks] = vy;
+            out[n + int64_t(r) * rs + int64_t(k) * ks] = vx;
+        }
+    }
+
     // Face weights of the order-8 central derivative written as a difference of face sums:
     // D8 f(j) = F(j + 1/2) - F(j - 1/2) with F(j + 1/2) = sum_e w_e f(j + e), e = -3..4,
     // w_e = sum of c_d over d >= max(e, 1 - e), c = (4/5, -1/5, 4/105, -1/280) (the sum in
@@ -1057,4 +1107,17 @@ extern "C" int amb_learned_spectral_combine(const void* phi_hat, const void* xi_
         float(noise_mag), size_t(n), static_cast<float2*>(out_y), static_cast<float2*>(out_x));
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_spectral_combine", e);
+}
+
+extern "C" int amb_learned_noise_spectral(int nrows, int ncols, uint64_t seed, const int64_t* step, void* out,
+                                          int64_t row_stride, int64_t col_stride, void* stream)
+{
+    if (!step || !out || nrows < 1 || ncols < 2 || row_stride < 1 || col_stride < 1)
+        return fail_invalid("amb_learned_noise_spectral: bad arguments");
+    const int64_t n = int64_t(nrows) * (ncols / 2 + 1);
+    const int grid = int(std::min<int64_t>((n + 255) / 256, int64_t(sm_count()) * 8));
+    learned_noise_spectral_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<float2*>(out), nrows, ncols, row_stride, col_stride, n, seed ^ 0x5bd1e995a5a5a5a5ull, step);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_noise_spectral", e);
 }

@@ -305,6 +305,14 @@ int amb_learned_update(const float* flux, const float* extra, int nrows, int nco
                        double dy, const float* xi, double noise_mag, int32_t* phi_q, float* phi_f, double bound,
                        int* flag, int64_t* step_to_advance, void* stream);
 
+/* The rfft2 spectra of two real white-noise fields (unit variance per site), drawn directly in
+ * the spectral domain: complex64 out[2][nrows][ncols/2+1], mode (r, k) of component c at element
+ * c*nrows*(ncols/2+1) + r*row_stride + k*col_stride. Complex normals with E|z|^2 = nrows*ncols,
+ * Hermitian-consistent in the k = 0 and k = ncols/2 columns (so an inverse real FFT sees the
+ * spectrum of a real field); Philox keyed (seed, *step, mode). */
+int amb_learned_noise_spectral(int nrows, int ncols, uint64_t seed, const int64_t* step, void* out,
+                               int64_t row_stride, int64_t col_stride, void* stream);
+
 /* Spectral step of the learned stepper's linear part and noise: for n complex rfft2 modes
  * (complex64 arrays), out_y = phi_hat * my + noise_mag * xi_hat_y * ny and
  * out_x = phi_hat * mx + noise_mag * xi_hat_x * nx, xi_hat = [2][n] (y then x) or NULL.

@@ -414,3 +414,26 @@ def test_spectral_combine_kernel():
         if x_in is not None:
             ey, ex = ey + 0.7 * x_in[0] * ny_, ex + 0.7 * x_in[1] * nx_
         assert float((out[0] - ey).abs().max()) < 1e-5 and float((out[1] - ex).abs().max()) < 1e-5
+
+
+def test_spectral_noise_is_the_spectrum_of_real_white_noise():
+    """amb_learned_noise_spectral: Hermitian-consistent (a real inverse FFT and back returns it),
+    unit variance per site in real space, flat mean power over modes, and keyed by the step."""
+    torch, L, N = mods()
+    H, W = 96, 128
+    nk = W // 2 + 1
+    step = torch.tensor([3], dtype=torch.int64, device="cuda")
+    out = torch.empty(2, H, nk, dtype=torch.complex64, device="cuda")
+    strm = torch.cuda.current_stream().cuda_stream
+    assert N.lib().amb_learned_noise_spectral(H, W, 11, step.data_ptr(), out.data_ptr(), nk, 1, strm) == 0
+    real = torch.fft.irfft2(out, s=(H, W))
+    back = torch.fft.rfft2(real)
+    assert float((back - out).abs().max()) < 1e-3 * float(out.abs().max())
+    v = float(real.var())
+    assert abs(v - 1.0) < 0.05, v
+    p = (out.abs() ** 2).mean(dim=(0,)).cpu().numpy()
+    assert abs(p[1:-1, 1:-1].mean() / (H * W) - 1) < 0.05
+    out2 = torch.empty_like(out)
+    step.fill_(4)
+    assert N.lib().amb_learned_noise_spectral(H, W, 11, step.data_ptr(), out2.data_ptr(), nk, 1, strm) == 0
+    assert not torch.equal(out, out2)
