@@ -648,13 +648,6 @@ class LearnedStepper:
         """Exact sum of the fixed-point field (integer)."""
         return int(self.phi_q.to(dtype=_torch().int64).sum().item())
 
-    def _flux(self):
-        """Deterministic flux of a macro step from the current state (network + linear part)."""
-        flux = self.net.forward(network_input(self.phi_f.unsqueeze(0), self.params))
-        if getattr(self.net, "linear_split", False):
-            flux = flux + self._linear.flux(self.phi_f.unsqueeze(0))
-        return flux
-
     def _apply(self, noisy: bool) -> None:
         """Network flux, plus (one spectral pass) the linear part and the filtered noise flux,
         then the exactly conservative fixed-point update."""
@@ -723,28 +716,38 @@ class LearnedStepper:
         sim.run(nsteps)
         self._set_from_float(sim.field_tensor)
 
-    def _check_step(self) -> bool:
-        """One deterministic macro step learned vs plain from the current state; returns
-        whether the relative residual of the increments is within tol (the state is not
-        advanced)."""
+    def _residual(self, start):
+        """Relative residual (device scalar) of one deterministic macro step, learned vs 50
+        plain steps, from the state ``start`` [H, W], enqueued on the current stream. A
+        non-finite plain or learned increment gives a non-finite residual."""
         torch = _torch()
-        start = self.phi_f.clone()
         sim = self._check_sim
         sim.field_tensor.copy_(start)
         if sim._residual is not None:
             sim._residual.zero_()
-        sim.run(self.K)
+        sim._launch(self.K)
         dplain = sim.field_tensor.float() - start
-        dpred = -self.dtk * divergence(self._flux(), self.stencil.dx, self.stencil.dy)[0]
+        flux = self.net.forward(network_input(start.unsqueeze(0), self.params))
+        if getattr(self.net, "linear_split", False):
+            flux = flux + self._linear.flux(start.unsqueeze(0))
+        dpred = -self.dtk * divergence(flux, self.stencil.dx, self.stencil.dy)[0]
         if self._wres is not None:
             dpred, dplain = lowpass(dpred, self._wres), lowpass(dplain, self._wres)
         num = torch.linalg.vector_norm(dpred - dplain)
         # the increment's norm, floored at atol RMS per site so that near-static states
         # (tiny increments) are judged by the absolute error
         den = torch.clamp(torch.linalg.vector_norm(dplain), min=self.atol * math.sqrt(dplain.numel()) + 1e-30)
-        res = float((num / den).item())
+        return num / den
+
+    def _accept(self, res: float) -> bool:
         self.residuals.append(res)
         return res <= self.tol and math.isfinite(res)
+
+    def _check_step(self) -> bool:
+        """One deterministic macro step learned vs plain from the current state; returns
+        whether the relative residual of the increments is within tol (the state is not
+        advanced)."""
+        return self._accept(float(self._residual(self.phi_f.clone()).item()))
 
     def advance(self, n_macro: int) -> None:
         """Advance n_macro macro steps (each K Euler steps)."""
