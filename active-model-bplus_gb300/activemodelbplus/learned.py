@@ -516,7 +516,6 @@ class LinearPart:
         self.nx_ = torch.from_numpy(np.broadcast_to(g * sym_x, full).astype(np.complex64)).to(dev)
         self._layout = None
         self._filters = None
-        self._noise_buf = None
 
     def flux(self, phi):
         """Linear part only: phi [B, H, W] -> G [B, 2, H, W] (component 0 = y face, 1 = x face)."""
@@ -528,10 +527,12 @@ class LinearPart:
 
     def extra(self, phi, xi, noise_mag: float, out, spectral_noise=None):
         """Linear part of phi [H, W] plus the noise flux of xi [2, H, W] (or None) into out [2, H, W]:
-        forward FFTs, one combining kernel (``amb_learned_spectral_combine``), two inverse FFTs.
-        ``spectral_noise=(seed, step)`` draws the noise spectrum directly
-        (``amb_learned_noise_spectral``, keyed by the device step counter) instead of
-        transforming xi: statistically the same white noise, two forward FFTs fewer."""
+        forward FFTs, one combining kernel (``amb_learned_spectral_combine``), one batched
+        inverse FFT of both components (its 1/(H W) folded into the filters).
+        ``spectral_noise=(seed, step)`` draws the noise spectrum in the combining kernel
+        (``amb_learned_spectral_combine_noise``: the draw of ``amb_learned_noise_spectral``,
+        keyed by the device step counter) instead of transforming xi: statistically the same
+        white noise, two forward FFTs and one kernel fewer."""
         torch = _torch()
         spec = torch.fft.rfft2(phi)
         sxi = torch.fft.rfft2(xi) if xi is not None else None
@@ -546,28 +547,28 @@ class LinearPart:
         if sum((d - 1) * st for d, st in zip(spec.shape, layout)) + 1 != n or min(layout) < 1:
             layout = (spec.shape[1], 1)   # not dense in its own strides: work row-major
         if self._layout != layout:
-            self._filters = [torch.empty_strided(spec.shape, layout, dtype=spec.dtype, device=spec.device).copy_(f)
-                             for f in (self.my, self.mx, self.ny_, self.nx_)]
+            # the inverse transform's 1/(H W) is folded into the filters (irfft2 with norm="forward")
+            inv_n = 1.0 / (self.shape[0] * self.shape[1])
+            self._filters = [torch.empty_strided(spec.shape, layout, dtype=spec.dtype, device=spec.device)
+                             .copy_(f * inv_n) for f in (self.my, self.mx, self.ny_, self.nx_)]
             self._layout = layout
-        if spectral_noise is not None:
-            if self._noise_buf is None or tuple(self._noise_buf.stride()) != (n,) + layout:
-                self._noise_buf = torch.empty_strided((2,) + tuple(spec.shape), (n,) + layout, dtype=spec.dtype,
-                                                      device=spec.device)
-            seed, step = spectral_noise
-            _check(N.lib().amb_learned_noise_spectral(self.shape[0], self.shape[1], int(seed), _ptr(step),
-                                                      _ptr(self._noise_buf), layout[0], layout[1], _stream()))
-            sxi = self._noise_buf
         if tuple(spec.stride()) != layout:
             spec = torch.empty_strided(spec.shape, layout, dtype=spec.dtype, device=spec.device).copy_(spec)
-        if sxi is not None and (tuple(sxi.stride()[1:]) != layout or sxi.stride(0) != n):
-            sxi = torch.empty_strided(sxi.shape, (n,) + layout, dtype=sxi.dtype, device=sxi.device).copy_(sxi)
         comb = torch.empty_strided((2,) + tuple(spec.shape), (n,) + layout, dtype=spec.dtype, device=spec.device)
         my, mx, ny_, nx_ = self._filters
-        _check(N.lib().amb_learned_spectral_combine(
-            _ptr(spec), _ptr(sxi), _ptr(my), _ptr(mx), _ptr(ny_), _ptr(nx_),
-            float(noise_mag), n, _ptr(comb[0]), _ptr(comb[1]), _stream()))
-        torch.fft.irfft2(comb[0], s=self.shape, out=out[0])
-        torch.fft.irfft2(comb[1], s=self.shape, out=out[1])
+        if spectral_noise is not None:
+            seed, step = spectral_noise
+            _check(N.lib().amb_learned_spectral_combine_noise(
+                _ptr(spec), _ptr(my), _ptr(mx), _ptr(ny_), _ptr(nx_), float(noise_mag), self.shape[0],
+                self.shape[1], layout[0], layout[1], int(seed), _ptr(step), _ptr(comb[0]), _ptr(comb[1]),
+                _stream()))
+        else:
+            if sxi is not None and (tuple(sxi.stride()[1:]) != layout or sxi.stride(0) != n):
+                sxi = torch.empty_strided(sxi.shape, (n,) + layout, dtype=sxi.dtype, device=sxi.device).copy_(sxi)
+            _check(N.lib().amb_learned_spectral_combine(
+                _ptr(spec), _ptr(sxi), _ptr(my), _ptr(mx), _ptr(ny_), _ptr(nx_),
+                float(noise_mag), n, _ptr(comb[0]), _ptr(comb[1]), _stream()))
+        torch.fft.irfft2(comb, s=self.shape, norm="forward", out=out)
         return out
 
 
@@ -579,7 +580,12 @@ class LearnedStepper:
         field: initial field (ny, nx), ncols % 128 == 0.
         stencil, model: as for :class:`Integrator` (dx = dy = 1 is what the network saw).
         K: Euler steps per macro step (the K the network was trained for).
-        check_every: macro steps per verified span.
+        check_every: macro steps per verified span (the shortest interval between checks).
+        max_check_every: longest interval; after each accepted check whose residual is below
+            tol/4 the interval doubles up to this, a residual above tol/2 or a failed check
+            resets it to ``check_every``. ``None`` (or ``check_every``) keeps it fixed. A failed
+            check redoes its whole span with the plain integrator, so a longer interval trades
+            a costlier rollback for fewer checks.
         tol: largest accepted relative residual ||learned - plain|| / ||plain - start|| of the
             checked deterministic macro step's increments.
         residual_sigma: if > 0, compare Gaussian low-passed increments (width in sites).
@@ -596,6 +602,7 @@ class LearnedStepper:
     """
 
     def __init__(self, net: FluxNet, field, stencil, model, *, K: int = 50, seed: int = 0, check_every: int = 40,
+                 max_check_every: int | None = 320,
                  tol: float = 0.5, bound: float = 3.0, plain_precision: str = "f32", use_graph: bool = True,
                  filter_noise: bool = True, residual_sigma: float = 0.0, atol: float = 0.0,
                  spectral_noise: bool = True):
@@ -607,6 +614,9 @@ class LearnedStepper:
         self.dtk = self.K * self.stencil.dt
         self.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
         self.check_every = int(check_every)
+        self.max_check_every = max(self.check_every, int(max_check_every or check_every))
+        self.interval = self.check_every
+        self.checks = 0
         self.tol = float(tol)
         self.bound = float(bound)
         self.atol = float(atol)
@@ -617,6 +627,10 @@ class LearnedStepper:
         self.phi_q = torch.from_numpy(np.rint(host * FIX).astype(np.int32)).to(dev)
         self.phi_f = (self.phi_q.double() / FIX).float()
         self.params = model_params_tensor([self.model], dev)
+        # the network input of the current state: kept current by the update kernel inside a
+        # macro step and by _refresh_input wherever the field changes outside one
+        self._x = torch.zeros(1, 2, *self.shape, 8, dtype=torch.bfloat16, device=dev)
+        self._refresh_input()
         self.flag = torch.zeros(1, dtype=torch.int32, device=dev)
         self.step_dev = torch.zeros(1, dtype=torch.int64, device=dev)
         self.xi = torch.zeros(2, *self.shape, dtype=torch.float32, device=dev)
@@ -654,7 +668,7 @@ class LearnedStepper:
         torch = _torch()
         lib = N.lib()
         ny, nx = self.shape
-        net_flux = self.net.forward(network_input(self.phi_f.unsqueeze(0), self.params))
+        net_flux = self.net.forward(self._x)
         noisy = noisy and self.model.T > 0
         mag = math.sqrt(2.0 * self.model.T) * math.sqrt(1.0 / (self.dtk * self.stencil.dx * self.stencil.dy))
         xi_direct = None
@@ -671,10 +685,14 @@ class LearnedStepper:
             self._linear.extra(self.phi_f, self.xi, mag, self._extra)
         else:
             self._linear.extra(self.phi_f, None, 0.0, self._extra)
-        _check(lib.amb_learned_update(_ptr(net_flux), _ptr(self._extra), ny, nx, self.dtk, self.stencil.dx,
-                                      self.stencil.dy, _ptr(xi_direct), mag if xi_direct is not None else 0.0,
-                                      _ptr(self.phi_q), _ptr(self.phi_f), self.bound, _ptr(self.flag),
-                                      _ptr(self.step_dev), _stream()))
+        _check(lib.amb_learned_update_input(_ptr(net_flux), _ptr(self._extra), ny, nx, self.dtk, self.stencil.dx,
+                                            self.stencil.dy, _ptr(xi_direct), mag if xi_direct is not None else 0.0,
+                                            _ptr(self.phi_q), _ptr(self.phi_f), self.bound, _ptr(self.flag),
+                                            _ptr(self.step_dev), _ptr(self.params), _ptr(self._x), _stream()))
+
+    def _refresh_input(self) -> None:
+        _check(N.lib().amb_learned_input(_ptr(self.phi_f), _ptr(self.params), 1, self.shape[0], self.shape[1],
+                                         _ptr(self._x), _stream()))
 
     def _macro_step(self) -> None:
         """One learned macro step (network, noise, fixed-point update, step counter).
@@ -692,6 +710,7 @@ class LearnedStepper:
             torch.cuda.current_stream().wait_stream(side)
             self.phi_q.copy_(saved[0])
             self.phi_f.copy_((self.phi_q.double() / FIX).float())
+            self._refresh_input()
             self.step_dev.copy_(saved[1])
             self.flag.copy_(saved[2])
             g = torch.cuda.CUDAGraph()
@@ -706,6 +725,7 @@ class LearnedStepper:
     def _set_from_float(self, f) -> None:
         self.phi_q.copy_(torch_round_fix(f))
         self.phi_f.copy_((self.phi_q.double() / FIX).float())
+        self._refresh_input()
 
     def _run_plain(self, nsteps: int) -> None:
         sim = self._plain
@@ -753,16 +773,22 @@ class LearnedStepper:
         """Advance n_macro macro steps (each K Euler steps)."""
         left = int(n_macro)
         while left > 0:
-            span = min(self.check_every, left)
+            span = min(self.interval, left)
             snap_q = self.phi_q.clone()
             snap_step = self.step_dev.clone()
             self.flag.zero_()
             for _ in range(span - 1):
                 self._macro_step()
             ok = self._check_step() and int(self.flag.item()) == 0
+            self.checks += 1
             if ok:
                 self._macro_step()
                 ok = int(self.flag.item()) == 0
+            res = self.residuals[-1]
+            if ok and res < 0.25 * self.tol:
+                self.interval = min(2 * self.interval, self.max_check_every)
+            elif not ok or res > 0.5 * self.tol:
+                self.interval = self.check_every
             if ok:
                 self.learned_steps += span
             else:
@@ -861,7 +887,8 @@ def _timed(fn):
 
 def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: int | None = None, seed: int = 0,
                        check_every: int = 40, tol: float = 0.5, plain_seeds=(1, 2, 3), residual_sigma: float = 2.0,
-                       filter_noise: bool = True, atol: float = 0.0, learned_runs: int = 3) -> dict:
+                       filter_noise: bool = True, atol: float = 0.0, learned_runs: int = 3,
+                       max_check_every: int | None = 320) -> dict:
     """Time to ``t_end`` and end-state statistics of the learned stepper against the plain
     FP32 integrator (the faster of the Integrator and a one-replica CUDA-graph ensemble)
     from the same initial field: S(k) mean wavenumber (the reference notebook's
@@ -875,7 +902,8 @@ def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: 
     field = np.asarray(field, dtype=np.float64)
     phi0 = float(field.mean())
     res = {"t_end": t_end, "K": K, "shape": list(field.shape), "model": model.as_dict(), "tol": tol, "atol": atol,
-           "check_every": check_every, "residual_sigma": residual_sigma, "filter_noise": filter_noise, "plain": []}
+           "check_every": check_every, "max_check_every": max_check_every, "residual_sigma": residual_sigma,
+           "filter_noise": filter_noise, "plain": []}
     probe = max(1, min(nsteps, 20000))
     sim = Integrator(field, stencil, model, precision="f32", seed=0)
     t_int = _timed(lambda: sim.run(probe))
@@ -905,7 +933,8 @@ def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: 
     res["learned_runs"] = []
     for sd in range(seed, seed + max(1, int(learned_runs))):
         st = LearnedStepper(net, field, stencil, model, K=K, seed=sd, check_every=check_every, tol=tol,
-                            residual_sigma=residual_sigma, filter_noise=filter_noise, atol=atol)
+                            residual_sigma=residual_sigma, filter_noise=filter_noise, atol=atol,
+                            max_check_every=max_check_every)
         m0 = st.mass_q()
         sec = _timed(lambda: st.run_for_time(t_end))
         f = st.field
@@ -914,6 +943,7 @@ def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: 
                                     "k_peak": float(k[np.nanargmax(S)]), "droplets": count_droplets(f, phi0),
                                     "mass_q_drift": st.mass_q() - m0, "macro_steps": st.macro_steps,
                                     "learned_macro_steps": st.learned_steps, "fallback_spans": st.fallback_spans,
+                                    "checks": st.checks, "max_residual": max(st.residuals) if st.residuals else None,
                                     "median_residual": float(np.median(st.residuals)) if st.residuals else None})
         del st
     runs = res["learned_runs"]
@@ -959,6 +989,7 @@ def _main(argv=None) -> int:
     c.add_argument("--size", type=int, default=512)
     c.add_argument("--t-end", type=float, default=1000.0)
     c.add_argument("--check-every", type=int, default=40)
+    c.add_argument("--max-check-every", type=int, default=320)
     c.add_argument("--tol", type=float, default=0.5)
     c.add_argument("--seed", type=int, default=0)
     c.add_argument("--temperature", type=float, default=0.05)
@@ -983,7 +1014,8 @@ def _main(argv=None) -> int:
     field = -0.4 + 0.01 * rng.standard_normal((a.size, a.size))
     model = Model(a=-0.25, b=0, c=0.25, kappa=1, lamb=-1, zeta=-4, T=a.temperature)
     res = compare_with_plain(net, field, Stencil(1e-3, 1, 1), model, t_end=a.t_end, seed=a.seed,
-                             check_every=a.check_every, tol=a.tol, residual_sigma=a.residual_sigma,
+                             check_every=a.check_every, max_check_every=a.max_check_every, tol=a.tol,
+                             residual_sigma=a.residual_sigma,
                              filter_noise=not a.no_noise_filter, atol=a.atol,
                              plain_seeds=tuple(int(v) for v in a.plain_seeds.split(",")))
     print(json.dumps(res))

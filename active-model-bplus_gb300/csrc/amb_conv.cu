@@ -715,43 +715,89 @@ namespace
     // nrows - r, and the self-conjugate modes (r = 0, r = nrows/2) are real with the same
     // variance. One Philox call per (r, k) (keyed by the lower of r and nrows - r in those
     // columns) gives both components.
+    __device__ __forceinline__ void spectral_noise_mode(uint64_t seed, int64_t st, int r, int k, int nrows, int ncols,
+                                                        float2& vy, float2& vx)
+    {
+        const float s_half = sqrtf(0.5f * float(nrows) * float(ncols));
+        const float s_full = sqrtf(float(nrows) * float(ncols));
+        const bool herm = k == 0 || (ncols % 2 == 0 && k == ncols / 2);
+        int rr = r;
+        bool conj = false;
+        if (herm && r > nrows / 2)
+        {
+            rr = nrows - r;
+            conj = true;
+        }
+        const amb::U4 b = amb::noise_bits(seed, st, rr, 4 * k, 0);
+        const float2 z0 = amb::box_muller_f32(b.x, b.y), z1 = amb::box_muller_f32(b.z, b.w);
+        vy = make_float2(z0.x * s_half, z0.y * s_half);
+        vx = make_float2(z1.x * s_half, z1.y * s_half);
+        if (herm && (rr == 0 || (nrows % 2 == 0 && rr == nrows / 2)))
+        {
+            vy = make_float2(z0.x * s_full, 0.f);
+            vx = make_float2(z1.x * s_full, 0.f);
+        }
+        if (conj)
+        {
+            vy.y = -vy.y;
+            vx.y = -vx.y;
+        }
+    }
+
     __global__ void learned_noise_spectral_kernel(float2* __restrict__ out, int nrows, int ncols, int64_t rs,
                                                   int64_t ks, int64_t n, uint64_t seed,
                                                   const int64_t* __restrict__ step)
     {
         const int nk = ncols / 2 + 1;
         const int64_t st = *step;
-        const float s_half = sqrtf(0.5f * float(nrows) * float(ncols));
-        const float s_full = sqrtf(float(nrows) * float(ncols));
         const int64_t total = int64_t(nrows) * nk;
         for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total;
              i += int64_t(gridDim.x) * blockDim.x)
         {
             const int r = int(i / nk), k = int(i - int64_t(r) * nk);
-            const bool herm = k == 0 || (ncols % 2 == 0 && k == ncols / 2);
-            int rr = r;
-            bool conj = false;
-            if (herm && r > nrows / 2)
-            {
-                rr = nrows - r;
-                conj = true;
-            }
-            const amb::U4 b = amb::noise_bits(seed, st, rr, 4 * k, 0);
-            const float2 z0 = amb::box_muller_f32(b.x, b.y), z1 = amb::box_muller_f32(b.z, b.w);
-            float2 vy = make_float2(z0.x * s_half, z0.y * s_half);
-            float2 vx = make_float2(z1.x * s_half, z1.y * s_half);
-            if (herm && (rr == 0 || (nrows % 2 == 0 && rr == nrows / 2)))
-            {
-                vy = make_float2(z0.x * s_full, 0.f);
-                vx = make_float2(z1.x * s_full, 0.f);
-            }
-            if (conj)
-            {
-                vy.y = -vy.y;
-                vx.y = -vx.y;
-            }
+            float2 vy, vx;
+            spectral_noise_mode(seed, st, r, k, nrows, ncols, vy, vx);
             out[int64_t(r) * rs + int64_t(k) * ks] = vy;
             out[n + int64_t(r) * rs + int64_t(k) * ks] = vx;
+        }
+    }
+
+    // The spectral combine with the noise spectrum drawn in place (the draw of
+    // learned_noise_spectral_kernel for the same seed and step): the spectra are dense in
+    // memory with row stride rs and column stride ks, one of them 1.
+    __global__ void spectral_combine_noise_kernel(const float2* __restrict__ phi_hat, const float2* __restrict__ my,
+                                                  const float2* __restrict__ mx, const float2* __restrict__ ny_,
+                                                  const float2* __restrict__ nx_, float noise_mag, int nrows,
+                                                  int ncols, int64_t rs, int64_t ks, uint64_t seed,
+                                                  const int64_t* __restrict__ step, float2* __restrict__ out_y,
+                                                  float2* __restrict__ out_x)
+    {
+        const int64_t n = int64_t(nrows) * (ncols / 2 + 1);
+        const int64_t st = *step;
+        for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        {
+            int r, k;
+            if (ks == 1)
+            {
+                r = int(i / rs);
+                k = int(i - int64_t(r) * rs);
+            }
+            else
+            {
+                k = int(i / ks);
+                r = int(i - int64_t(k) * ks);
+            }
+            float2 u, v;
+            spectral_noise_mode(seed, st, r, k, nrows, ncols, u, v);
+            const float2 p = phi_hat[i], a = my[i], b = mx[i], c = ny_[i], d = nx_[i];
+            float2 y = make_float2(p.x * a.x - p.y * a.y, p.x * a.y + p.y * a.x);
+            float2 x = make_float2(p.x * b.x - p.y * b.y, p.x * b.y + p.y * b.x);
+            y.x += noise_mag * (u.x * c.x - u.y * c.y);
+            y.y += noise_mag * (u.x * c.y + u.y * c.x);
+            x.x += noise_mag * (v.x * d.x - v.y * d.y);
+            x.y += noise_mag * (v.x * d.y + v.y * d.x);
+            out_y[i] = y;
+            out_x[i] = x;
         }
     }
 
@@ -793,7 +839,7 @@ namespace
         }
         float q = __fmul_rn(scale, v);
         q = q > 1e9f ? 1e9f : (q < -1e9f ? -1e9f : q);
-        return __float2ll_rn(q);
+        return (long long)__float2int_rn(q);  // |q| <= 1e9 < 2^31: the same value as a 64-bit conversion
     }
 
     // phi_q -= sum of integer face increments (each face computed identically by the two
@@ -802,7 +848,8 @@ namespace
                                           const float* __restrict__ xi, int nrows, int ncols, float scale_y,
                                           float scale_x, float noise_mag, int32_t* __restrict__ phi_q,
                                           float* __restrict__ phi_f, long long bound, int* __restrict__ flag,
-                                          int64_t* __restrict__ advance)
+                                          int64_t* __restrict__ advance, const float* __restrict__ params,
+                                          uint4* __restrict__ x_next)
     {
         // the next macro step's noise key (nothing in this launch reads it)
         if (advance && blockIdx.x == 0 && threadIdx.x == 0) *advance += 1;
@@ -830,7 +877,15 @@ namespace
                 q = q > bound ? bound : (q < -bound ? -bound : q);
             }
             phi_q[i] = int32_t(q);
-            phi_f[i] = float(double(q) * (1.0 / 16777216.0));
+            const float f = float(double(q) * (1.0 / 16777216.0));
+            phi_f[i] = f;
+            if (x_next)  // channel chunk 0 of the next network input, as learned_input_kernel forms it
+            {
+                const __nv_bfloat16 hi = __float2bfloat16_rn(f);
+                const float lo = (f - __bfloat162float(hi)) * 256.f;
+                x_next[i] = make_uint4(pack_bf16x2(__bfloat162float(hi), lo), pack_bf16x2(params[0] * 0.25f, params[1]),
+                                       pack_bf16x2(params[2] * 10.f, 0.f), 0u);
+            }
         }
     }
 
@@ -1073,13 +1128,11 @@ extern "C" int amb_learned_noise(int nrows, int ncols, uint64_t seed, const int6
     return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_noise", e);
 }
 
-extern "C" int amb_learned_update(const float* flux, const float* extra, int nrows, int ncols, double dt_macro,
-                                  double dx, double dy, const float* xi, double noise_mag, int32_t* phi_q,
-                                  float* phi_f, double bound, int* flag, int64_t* step_to_advance, void* stream)
+static int learned_update_launch(const float* flux, const float* extra, int nrows, int ncols, double dt_macro,
+                                 double dx, double dy, const float* xi, double noise_mag, int32_t* phi_q, float* phi_f,
+                                 double bound, int* flag, int64_t* step_to_advance, const float* params, void* x_next,
+                                 void* stream)
 {
-    if (!flux || !phi_q || !phi_f || !flag || nrows < 1 || ncols < 1 || !(dt_macro > 0) || !(dx > 0) ||
-        !(dy > 0) || !(noise_mag >= 0) || !(bound > 0))
-        return fail_invalid("amb_learned_update: bad arguments");
     auto s = static_cast<cudaStream_t>(stream);
     const size_t n = size_t(nrows) * ncols;
     const int grid = int(std::min<size_t>((n + 255) / 256, size_t(sm_count()) * 16));
@@ -1089,9 +1142,39 @@ extern "C" int amb_learned_update(const float* flux, const float* extra, int nro
     learned_update_kernel<<<grid, 256, 0, s>>>(flux, extra, noisy ? xi : nullptr, nrows, ncols,
                                                float(dt_macro / dy * fix), float(dt_macro / dx * fix),
                                                noisy ? float(noise_mag) : 0.f, phi_q, phi_f, (long long)qb, flag,
-                                               step_to_advance);
+                                               step_to_advance, params, static_cast<uint4*>(x_next));
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_update", e);
+}
+
+static bool learned_update_args_ok(const float* flux, const int32_t* phi_q, const float* phi_f, const int* flag,
+                                   int nrows, int ncols, double dt_macro, double dx, double dy, double noise_mag,
+                                   double bound)
+{
+    return flux && phi_q && phi_f && flag && nrows >= 1 && ncols >= 1 && dt_macro > 0 && dx > 0 && dy > 0 &&
+           noise_mag >= 0 && bound > 0;
+}
+
+extern "C" int amb_learned_update(const float* flux, const float* extra, int nrows, int ncols, double dt_macro,
+                                  double dx, double dy, const float* xi, double noise_mag, int32_t* phi_q,
+                                  float* phi_f, double bound, int* flag, int64_t* step_to_advance, void* stream)
+{
+    if (!learned_update_args_ok(flux, phi_q, phi_f, flag, nrows, ncols, dt_macro, dx, dy, noise_mag, bound))
+        return fail_invalid("amb_learned_update: bad arguments");
+    return learned_update_launch(flux, extra, nrows, ncols, dt_macro, dx, dy, xi, noise_mag, phi_q, phi_f, bound,
+                                 flag, step_to_advance, nullptr, nullptr, stream);
+}
+
+extern "C" int amb_learned_update_input(const float* flux, const float* extra, int nrows, int ncols, double dt_macro,
+                                        double dx, double dy, const float* xi, double noise_mag, int32_t* phi_q,
+                                        float* phi_f, double bound, int* flag, int64_t* step_to_advance,
+                                        const float* params, void* x_next, void* stream)
+{
+    if (!learned_update_args_ok(flux, phi_q, phi_f, flag, nrows, ncols, dt_macro, dx, dy, noise_mag, bound) ||
+        !params || !x_next || (reinterpret_cast<uintptr_t>(x_next) & 15) != 0)
+        return fail_invalid("amb_learned_update_input: bad arguments");
+    return learned_update_launch(flux, extra, nrows, ncols, dt_macro, dx, dy, xi, noise_mag, phi_q, phi_f, bound,
+                                 flag, step_to_advance, params, x_next, stream);
 }
 
 extern "C" int amb_learned_spectral_combine(const void* phi_hat, const void* xi_hat, const void* my, const void* mx,
@@ -1120,4 +1203,25 @@ extern "C" int amb_learned_noise_spectral(int nrows, int ncols, uint64_t seed, c
         static_cast<float2*>(out), nrows, ncols, row_stride, col_stride, n, seed ^ 0x5bd1e995a5a5a5a5ull, step);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_noise_spectral", e);
+}
+
+extern "C" int amb_learned_spectral_combine_noise(const void* phi_hat, const void* my, const void* mx, const void* ny,
+                                                  const void* nx, double noise_mag, int nrows, int ncols,
+                                                  int64_t row_stride, int64_t col_stride, uint64_t seed,
+                                                  const int64_t* step, void* out_y, void* out_x, void* stream)
+{
+    const int64_t nk = ncols / 2 + 1;
+    const bool row_major = col_stride == 1 && row_stride == nk;
+    const bool col_major = row_stride == 1 && col_stride == nrows;
+    if (!phi_hat || !my || !mx || !ny || !nx || !step || !out_y || !out_x || nrows < 1 || ncols < 2 ||
+        !(row_major || col_major))
+        return fail_invalid("amb_learned_spectral_combine_noise: bad arguments (spectra must be dense)");
+    const int64_t n = int64_t(nrows) * nk;
+    const int grid = int(std::min<int64_t>((n + 255) / 256, int64_t(sm_count()) * 8));
+    spectral_combine_noise_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const float2*>(phi_hat), static_cast<const float2*>(my), static_cast<const float2*>(mx),
+        static_cast<const float2*>(ny), static_cast<const float2*>(nx), float(noise_mag), nrows, ncols, row_stride,
+        col_stride, seed ^ 0x5bd1e995a5a5a5a5ull, step, static_cast<float2*>(out_y), static_cast<float2*>(out_x));
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? AMB_OK : fail_cuda("amb_learned_spectral_combine_noise", e);
 }

@@ -478,7 +478,8 @@ def run_learned_launches(args):
 def run_learned_steps(args):
     """N macro steps (K = 50 Euler steps each) of the learned stepper on the 512^2 field of the
     learned workload, after 40 untimed ones (graph capture, first checks); wall time per macro
-    step, CUDA-synchronised, including its residual checks (one per 40 macro steps)."""
+    step, CUDA-synchronised, including its residual checks (adaptive: one per 40 to 320 macro
+    steps)."""
     import torch
     from activemodelbplus import learned as L
     from activemodelbplus.integrator import Model, Stencil
@@ -514,7 +515,8 @@ def run_learned(args):
     out = {"metric": f"learned vs plain FP32 time to t={args.t_end:g} (512^2 AMB+), speed-up", "value": res["speedup"],
            "unit": "x", "higher_is_better": True, "n_gpus": 1, "dtype": "bf16 network / int32 fixed-point field",
            "data": "synthetic", "config": {"workload": "learned_time_to_t", "size": 512, "K": 50,
-                                           "t_end": args.t_end, "check_every": res["check_every"], "tol": res["tol"]},
+                                           "t_end": args.t_end, "check_every": res["check_every"],
+                                           "max_check_every": res["max_check_every"], "tol": res["tol"]},
            "plain_seconds": res["plain_seconds_min"], "learned_seconds": res["learned_seconds_min"],
            "plain_path": res["plain_path"], "k_avg_plain_mean": res["plain_k_avg_mean"],
            "k_avg_plain_std": res["plain_k_avg_std"], "k_avg_learned_mean": res["learned_k_avg_mean"],
@@ -523,7 +525,8 @@ def run_learned(args):
            "droplets_learned": [r["droplets"] for r in res["learned_runs"]],
            "mass_q_drift_learned_max": res["learned_mass_q_drift_max"],
            "learned_macro_steps": [r["learned_macro_steps"] for r in res["learned_runs"]],
-           "fallback_spans": res["learned_fallback_spans"], "clocks": clocks.summary()}
+           "fallback_spans": res["learned_fallback_spans"], "checks": [r["checks"] for r in res["learned_runs"]],
+           "max_residual": max(r["max_residual"] for r in res["learned_runs"]), "clocks": clocks.summary()}
     print(json.dumps(out), flush=True)
 
 

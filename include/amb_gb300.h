@@ -305,6 +305,14 @@ int amb_learned_update(const float* flux, const float* extra, int nrows, int nco
                        double dy, const float* xi, double noise_mag, int32_t* phi_q, float* phi_f, double bound,
                        int* flag, int64_t* step_to_advance, void* stream);
 
+/* amb_learned_update that also writes channel chunk 0 of the next network input (x_next, bf16
+ * chunk planes [2][nrows][ncols][8], 16-byte aligned) from the updated field and params
+ * (zeta, lambda, T), exactly as amb_learned_input does; chunk 1 (zeros) is left untouched. */
+int amb_learned_update_input(const float* flux, const float* extra, int nrows, int ncols, double dt_macro,
+                             double dx, double dy, const float* xi, double noise_mag, int32_t* phi_q, float* phi_f,
+                             double bound, int* flag, int64_t* step_to_advance, const float* params, void* x_next,
+                             void* stream);
+
 /* The rfft2 spectra of two real white-noise fields (unit variance per site), drawn directly in
  * the spectral domain: complex64 out[2][nrows][ncols/2+1], mode (r, k) of component c at element
  * c*nrows*(ncols/2+1) + r*row_stride + k*col_stride. Complex normals with E|z|^2 = nrows*ncols,
@@ -321,6 +329,15 @@ int amb_learned_noise_spectral(int nrows, int ncols, uint64_t seed, const int64_
 int amb_learned_spectral_combine(const void* phi_hat, const void* xi_hat, const void* my, const void* mx,
                                  const void* ny, const void* nx, double noise_mag, int64_t n, void* out_y,
                                  void* out_x, void* stream);
+
+/* amb_learned_spectral_combine with xi_hat drawn in place: the draw amb_learned_noise_spectral
+ * makes for the same seed and *step. All spectra are [nrows][ncols/2+1] complex64 in one dense
+ * layout given by its strides (row-major: col_stride 1, row_stride ncols/2+1; column-major:
+ * row_stride 1, col_stride nrows); other layouts are rejected. */
+int amb_learned_spectral_combine_noise(const void* phi_hat, const void* my, const void* mx, const void* ny,
+                                       const void* nx, double noise_mag, int nrows, int ncols, int64_t row_stride,
+                                       int64_t col_stride, uint64_t seed, const int64_t* step, void* out_y,
+                                       void* out_x, void* stream);
 
 #ifdef __cplusplus
 }

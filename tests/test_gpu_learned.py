@@ -437,3 +437,65 @@ def test_spectral_noise_is_the_spectrum_of_real_white_noise():
     step.fill_(4)
     assert N.lib().amb_learned_noise_spectral(H, W, 11, step.data_ptr(), out2.data_ptr(), nk, 1, strm) == 0
     assert not torch.equal(out, out2)
+
+
+def test_spectral_combine_with_drawn_noise_matches_the_two_kernel_form():
+    """amb_learned_spectral_combine_noise equals amb_learned_noise_spectral followed by
+    amb_learned_spectral_combine (same draw, same arithmetic), in row- and column-major
+    spectrum layouts; a layout that is not dense is rejected."""
+    torch, L, N = mods()
+    g = torch.Generator(device="cpu").manual_seed(5)
+    H, W = 48, 256
+    nk = W // 2 + 1
+    strm = torch.cuda.current_stream().cuda_stream
+    step = torch.tensor([17], dtype=torch.int64, device="cuda")
+    for layout in ((nk, 1), (1, H)):
+        n = H * nk
+        mk = lambda lead=(): torch.empty_strided(lead + (H, nk), ((n,) if lead else ()) + layout,
+                                                 dtype=torch.complex64, device="cuda")
+        arrs = []
+        for _ in range(5):
+            a = mk()
+            a.copy_(torch.randn(H, nk, generator=g, dtype=torch.complex64))
+            arrs.append(a)
+        phi, my, mx, ny_, nx_ = arrs
+        xi, ref, got = mk((2,)), mk((2,)), mk((2,))
+        assert N.lib().amb_learned_noise_spectral(H, W, 9, step.data_ptr(), xi.data_ptr(), layout[0], layout[1],
+                                                  strm) == 0
+        assert N.lib().amb_learned_spectral_combine(phi.data_ptr(), xi.data_ptr(), my.data_ptr(), mx.data_ptr(),
+                                                    ny_.data_ptr(), nx_.data_ptr(), 0.3, n, ref[0].data_ptr(),
+                                                    ref[1].data_ptr(), strm) == 0
+        assert N.lib().amb_learned_spectral_combine_noise(phi.data_ptr(), my.data_ptr(), mx.data_ptr(),
+                                                          ny_.data_ptr(), nx_.data_ptr(), 0.3, H, W, layout[0],
+                                                          layout[1], 9, step.data_ptr(), got[0].data_ptr(),
+                                                          got[1].data_ptr(), strm) == 0, N.last_error()
+        scale = float(ref.abs().max())
+        assert float((got - ref).abs().max()) <= 1e-6 * scale
+    assert N.lib().amb_learned_spectral_combine_noise(phi.data_ptr(), my.data_ptr(), mx.data_ptr(), ny_.data_ptr(),
+                                                      nx_.data_ptr(), 0.3, H, W, 2 * nk, 1, 9, step.data_ptr(),
+                                                      got[0].data_ptr(), got[1].data_ptr(), strm) != 0
+
+
+def test_update_writes_the_next_network_input():
+    """amb_learned_update_input leaves in the stepper's input buffer exactly what
+    amb_learned_input makes from the updated field (eager and graph-replayed macro steps,
+    and after a fallback span)."""
+    torch, L, N = mods()
+    from activemodelbplus.integrator import Model, Stencil
+    field = -0.4 + 0.05 * np.random.default_rng(4).standard_normal((64, 256))
+    net = L.FluxNet(seed=6)
+    for w in net.weights:
+        w.mul_(0.1)
+    net.refresh()
+    m = Model(-0.25, 0, 0.25, 1, -1, -4, 0.05)
+    for graph in (False, True):
+        s = L.LearnedStepper(net, field, Stencil(1e-3, 1, 1), m, K=50, seed=2, check_every=3, tol=1e9,
+                             use_graph=graph)
+        s.advance(5)
+        ref = L.network_input(s.phi_f.unsqueeze(0), s.params)
+        assert torch.equal(s._x.view(torch.int16), ref.view(torch.int16))
+    s.tol = -1.0  # every check fails: the span is redone by the plain integrator
+    s.advance(3)
+    assert s.fallback_spans >= 1
+    ref = L.network_input(s.phi_f.unsqueeze(0), s.params)
+    assert torch.equal(s._x.view(torch.int16), ref.view(torch.int16))
