@@ -75,6 +75,11 @@ def parse_args(argv=None):
     ap.add_argument("--pairs", type=int, default=0, help="with --kernel sliding: warp pairs per CTA")
     ap.add_argument("--launches", type=int, default=0,
                     help="profiling driver: run this many bare step launches through the C ABI and exit")
+    ap.add_argument("--sweep", action="store_true",
+                    help="precision/bandwidth sweep: f64, f32c and f32 from one field at each --sweep-sizes, "
+                         "--sweep-steps steps; throughput and max/RMS/S(k) error against the FP64 run")
+    ap.add_argument("--sweep-sizes", default="4096,8192")
+    ap.add_argument("--sweep-steps", type=int, default=10000)
     return ap.parse_args(argv)
 
 
@@ -420,6 +425,62 @@ def run_launches(args, w):
     print(json.dumps({"launches": args.launches, "size": w["ny"], "precision": args.precision}))
 
 
+def run_sweep(args):
+    """Precision/bandwidth sweep on the bench workload's parameters (zeta=-1, lambda=0.5, T=0.05,
+    phi0=-0.4+0.01N(0,1), numpy seed 2024) at each size: the same field and Philox key run
+    --sweep-steps steps in FP64 (the path pinned to the reference at 1e-12), in FP32 with the
+    bf16-compensated update (f32c) and in plain FP32, each timed with CUDA events around one
+    Integrator.run (the autotuner runs in the constructor, outside the timed region). Prints one
+    JSON line per (size, precision): Gsite-updates/s, algorithmic GB/s (16 B/site FP64, 8 B/site
+    FP32) and its fraction of the measured HBM copy bandwidth, and against the FP64 end state the
+    max and RMS |delta phi|, the relative L2 error of S(k) over the notebook's bins and the
+    relative error of the S(k) mean wavenumber."""
+    import copy
+    import torch
+    from activemodelbplus.analysis import mean_wavenumber, structure_factor
+    from activemodelbplus.integrator import Integrator, Model, Stencil
+    peak, peak_kind = peaks()
+    for size in [int(v) for v in args.sweep_sizes.split(",")]:
+        a2 = copy.copy(args)
+        a2.size = size
+        w = workload(a2)
+        field = initial_field(w)
+        stencil = Stencil(w["dt"], w["dx"], w["dy"])
+        model = Model(w["a"], w["b"], w["c"], w["kappa"], w["lamb"], w["zeta"], w["T"])
+        ref = None
+        for prec in ("f64", "f32c", "f32"):
+            sim = Integrator(field, stencil, model, precision=prec, seed=w["seed"])
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with ClockSampler(torch.cuda.current_device()) as clocks:
+                e0.record()
+                sim.run(args.sweep_steps)
+                e1.record()
+                torch.cuda.synchronize()
+            sec = e0.elapsed_time(e1) / 1e3
+            end = sim.field_tensor.double().clone()
+            cfg = getattr(sim, "kernel_config", None)
+            del sim
+            gsite = size * size * args.sweep_steps / sec / 1e9
+            bps = 16 if prec == "f64" else 8
+            line = {"sweep": True, "size": size, "precision": prec, "steps": args.sweep_steps, "seconds": sec,
+                    "gsite_per_s": gsite, "gbs_algorithmic": gsite * bps, "hbm_frac": gsite * bps / peak,
+                    "peak_gbs": peak, "peak_source": peak_kind, "kernel_config": cfg, "clocks": clocks.summary()}
+            k, S, _ = structure_factor(end, w["dx"], w["dy"], phi0=w["phi0"])
+            if ref is None:
+                ref = (end, S, mean_wavenumber(k, S))
+            else:
+                d = end - ref[0]
+                m = np.isfinite(S) & np.isfinite(ref[1])
+                line.update({"max_abs_err_vs_f64": float(d.abs().max()),
+                             "rms_err_vs_f64": float(d.square().mean().sqrt()),
+                             "sk_rel_l2_err_vs_f64": float(np.linalg.norm(S[m] - ref[1][m]) / np.linalg.norm(ref[1][m])),
+                             "kavg_rel_err_vs_f64": abs(mean_wavenumber(k, S) - ref[2]) / ref[2]})
+            print(json.dumps(line), flush=True)
+        del ref
+        torch.cuda.empty_cache()
+
+
 def run_ensemble(args):
     """Batched ensemble: 256 replicas, sizes drawn from {128,192,256,384,512,768,1024}^2, zeta in
     [-4,4], lambda in [-1,1], phi0 in [-0.6,0.6], T in [0,0.1], a=-0.25 c=0.25 kappa=1, dt=1e-3,
@@ -541,6 +602,8 @@ def main():
         return run_launches(args, w)
     if args.ensemble:
         return run_ensemble(args)
+    if args.sweep:
+        return run_sweep(args)
     if args.learned:
         return run_learned(args)
     if args.learned_launches > 0:

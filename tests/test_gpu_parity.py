@@ -291,7 +291,9 @@ def test_noise_statistics_device():
 def test_fp32_paths_track_fp64(T):
     """FP32 storage vs FP64 on AMB+ (zeta=-1, lambda=0.5), 256^2, 2000 steps, same Philox
     noise. Bounds: F32C max|d| < 2e-5, F32 max|d| < 2e-4 (the F32C residual removes the
-    storage rounding that dominates plain F32 at T = 0)."""
+    storage rounding that dominates plain F32 at T = 0); the F32C structure factor within 1e-4
+    (relative L2 over the notebook's bins) of the FP64 one."""
+    from activemodelbplus.analysis import structure_factor
     I = lib_integrator()
     rng = np.random.default_rng(8)
     field = -0.4 + 0.01 * rng.standard_normal((256, 256))
@@ -300,10 +302,15 @@ def test_fp32_paths_track_fp64(T):
     ref.run(2000)
     f64 = ref.field
     errs = {}
+    _, s64, _ = structure_factor(f64, phi0=-0.4)
     for precision in ("f32", "f32c"):
         sim = I.Integrator(field, stencil, model, precision=precision, seed=5)
         sim.run(2000)
         errs[precision] = maxabs(sim.field - f64)
+        if precision == "f32c":
+            _, s32, _ = structure_factor(sim.field, phi0=-0.4)
+            m = np.isfinite(s64)
+            assert np.linalg.norm(s32[m] - s64[m]) / np.linalg.norm(s64[m]) < 1e-4
     assert errs["f32c"] < 2e-5
     assert errs["f32"] < 2e-4
     if T == 0.0:
