@@ -147,6 +147,11 @@ namespace amb
             float py8[4], px8[4];      // dyInv d_j, dxInv d_j (D8 J1)
             float ndy, jx1, jx3;       // J_l,y = ndy (sx(k) - sx(k-2)); J_l,x = jx1 (dx(k)+dx(k-2)) + jx3 dx(k-1)
             float dyInv, tx1, tx3;     // divTj = dyInv (sxJ(k-1)-sxJ(k-3)) + tx1 (dxJ(k-3)+dxJ(k-1)) + tx3 dxJ(k-2)
+            // duplicated pairs for the packed (f32x2) arithmetic on a lane's column pairs
+            float2 ny8p[4], py8p[4], magp;
+            float2 cp, bp, ap, nkappap, lambdap, zetap;  // c, b, a, -kappa, lambda, zeta
+            float2 ndyp, jx1p, jx3p, tx1p, tx3p, dyInvp;
+            float2 dtp, ndtp;                             // dt, -dt
             uint32_t rk0[10], rk1[10]; // Philox round keys of the seed
             __host__ __device__ explicit Coef(const StepParams& p)
             {
@@ -173,15 +178,42 @@ namespace amb
                     nx8[j] = float(-p.dxInv * d8_tap(j + 1));
                     py8[j] = float(p.dyInv * d8_tap(j + 1));
                     px8[j] = float(p.dxInv * d8_tap(j + 1));
+                    ny8p[j] = make_float2(ny8[j], ny8[j]);
+                    py8p[j] = make_float2(py8[j], py8[j]);
                 }
                 ndy = float(-p.dyInv);
                 jx1 = float(-0.1 * p.dxInv); jx3 = float(-0.3 * p.dxInv);
                 dyInv = float(p.dyInv);
                 tx1 = float(0.1 * p.dxInv); tx3 = float(0.3 * p.dxInv);
+                const auto dup = [](float v) { return make_float2(v, v); };
+                magp = dup(mag);
+                cp = dup(c); bp = dup(b); ap = dup(a); nkappap = dup(-kappa); lambdap = dup(lambda);
+                zetap = dup(zeta);
+                ndyp = dup(ndy); jx1p = dup(jx1); jx3p = dup(jx3); tx1p = dup(tx1); tx3p = dup(tx3);
+                dyInvp = dup(dyInv); dtp = dup(dt); ndtp = dup(-dt);
             }
         };
 
         __device__ __forceinline__ float4 lds4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+
+        // Packed FP32 pairs (sm_100+ f32x2): each lane rounds exactly as the scalar operation.
+        __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+
+        // One order-8 y derivative c . (r[5+j] - r[3-j]) of four columns, in column pairs, in the
+        // scalar code's operation order: c0 (r5 - r3), then fused c_j (r[5+j] - r[3-j]) + acc.
+        __device__ __forceinline__ void d8y_pairs(const float4 (&r)[9], const float2 (&c)[4], float2& lo, float2& hi)
+        {
+            const auto L = [](const float4& v) { return make_float2(v.x, v.y); };
+            const auto H = [](const float4& v) { return make_float2(v.z, v.w); };
+            lo = __fmul2_rn(c[0], sub2(L(r[5]), L(r[3])));
+            hi = __fmul2_rn(c[0], sub2(H(r[5]), H(r[3])));
+#pragma unroll
+            for (int j = 1; j < 4; ++j)
+            {
+                lo = __ffma2_rn(c[j], sub2(L(r[5 + j]), L(r[3 - j])), lo);
+                hi = __ffma2_rn(c[j], sub2(H(r[5 + j]), H(r[3 - j])), hi);
+            }
+        }
         __device__ __forceinline__ void sts4(float* p, const float (&v)[4])
         {
             *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
@@ -317,15 +349,20 @@ namespace amb
                 }
                 float mup[4], mua[4], jcy[4], jcx[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
+                for (int h2 = 0; h2 < 2; ++h2)  // column pairs (0, 1) and (2, 3), packed
                 {
-                    float f = f0[q];
-                    float poly = fmaf(fmaf(k.c, f, k.b), f, k.a) * f;
-                    mup[q] = fmaf(-k.kappa, lap[q], poly);
-                    mua[q] = k.lambda * fmaf(gy[q], gy[q], gx[q] * gx[q]);
-                    float zl = k.zeta * lap[q];
-                    jcy[q] = zl * gy[q];
-                    jcx[q] = zl * gx[q];
+                    const int q = 2 * h2;
+                    const float2 f = make_float2(f0[q], f0[q + 1]), l2 = make_float2(lap[q], lap[q + 1]);
+                    const float2 x2 = make_float2(gx[q], gx[q + 1]), y2 = make_float2(gy[q], gy[q + 1]);
+                    const float2 poly = __fmul2_rn(__ffma2_rn(__ffma2_rn(k.cp, f, k.bp), f, k.ap), f);
+                    const float2 mp = __ffma2_rn(k.nkappap, l2, poly);
+                    const float2 ma = __fmul2_rn(k.lambdap, __ffma2_rn(y2, y2, __fmul2_rn(x2, x2)));
+                    const float2 zl = __fmul2_rn(k.zetap, l2);
+                    const float2 cy = __fmul2_rn(zl, y2), cx = __fmul2_rn(zl, x2);
+                    mup[q] = mp.x; mup[q + 1] = mp.y;
+                    mua[q] = ma.x; mua[q + 1] = ma.y;
+                    jcy[q] = cy.x; jcy[q + 1] = cy.y;
+                    jcx[q] = cx.x; jcx[q + 1] = cx.y;
                 }
                 sts4(&sm.mup[ms][4 * lane], mup);
                 float(*h)[kCols] = sm.hand[kl & 1];
@@ -336,55 +373,42 @@ namespace amb
                 // Outputs start at local row 9 and read J1_y rows >= 5 (rounds >= 9); earlier rounds
                 // compute values nobody reads, which keeps the round one straight-line block.
                 {
-                    float m[9][4];
+                    float4 m[9];
 #pragma unroll
                     for (int i = 0; i < 8; ++i)
                     {
                         if (i == 4) continue;
                         int slot = ms - 8 + i;
                         slot += slot < 0 ? kMupRing : 0;
-                        float4 v = lds4(&sm.mup[slot][4 * lane]);
-                        m[i][0] = v.x; m[i][1] = v.y; m[i][2] = v.z; m[i][3] = v.w;
+                        m[i] = lds4(&sm.mup[slot][4 * lane]);
                     }
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) m[8][q] = mup[q];
-                    float xi[4] = {xin[0], xin[1], xin[2], xin[3]};
+                    m[4] = make_float4(0.f, 0.f, 0.f, 0.f);  // the centre tap has weight 0
+                    m[8] = make_float4(mup[0], mup[1], mup[2], mup[3]);
+                    const float2 xlo = make_float2(xin[0], xin[1]), xhi = make_float2(xin[2], xin[3]);
                     // noise of the next round's J1_y row, formed now so its Philox chain overlaps this round
                     normals<NOISE>(p, k, injected, wrap_index(t.r0 - 12 + kl, ny), gcol, 0, xin);
-                    float j1y[4];
-#pragma unroll
-                    for (int q = 0; q < 4; ++q)
-                    {
-                        float s = k.ny8[0] * (m[5][q] - m[3][q]);
-                        s = fmaf(k.ny8[1], m[6][q] - m[2][q], s);
-                        s = fmaf(k.ny8[2], m[7][q] - m[1][q], s);
-                        s = fmaf(k.ny8[3], m[8][q] - m[0][q], s);
-                        j1y[q] = fmaf(k.mag, xi[q], s);
-                    }
+                    float2 slo, shi;
+                    d8y_pairs(m, k.ny8p, slo, shi);
+                    slo = __ffma2_rn(k.magp, xlo, slo);
+                    shi = __ffma2_rn(k.magp, xhi, shi);
+                    const float j1y[4] = {slo.x, slo.y, shi.x, shi.y};
                     sts4(&sm.j1y[js][4 * lane], j1y);
                     // ---- DY8 at local row kl-8 from J1_y rows kl-12..kl-4 (read by outputs from round 17)
                     {
-                        float j[9][4];
+                        float4 j[9];
 #pragma unroll
                         for (int i = 0; i < 8; ++i)
                         {
                             if (i == 4) continue;
                             int slot = js - 8 + i;
                             slot += slot < 0 ? kJ1Ring : 0;
-                            float4 v = lds4(&sm.j1y[slot][4 * lane]);
-                            j[i][0] = v.x; j[i][1] = v.y; j[i][2] = v.z; j[i][3] = v.w;
+                            j[i] = lds4(&sm.j1y[slot][4 * lane]);
                         }
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) j[8][q] = j1y[q];
-                        float dy8[4];
-#pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                        {
-                            float d = k.py8[0] * (j[5][q] - j[3][q]);
-                            d = fmaf(k.py8[1], j[6][q] - j[2][q], d);
-                            d = fmaf(k.py8[2], j[7][q] - j[1][q], d);
-                            dy8[q] = fmaf(k.py8[3], j[8][q] - j[0][q], d);
-                        }
+                        j[4] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        j[8] = make_float4(j1y[0], j1y[1], j1y[2], j1y[3]);
+                        float2 dlo, dhi;
+                        d8y_pairs(j, k.py8p, dlo, dhi);
+                        const float dy8[4] = {dlo.x, dlo.y, dhi.x, dhi.y};
                         sts4(&h[3][4 * lane], dy8);
                     }
                 }
@@ -459,10 +483,14 @@ namespace amb
                         }
                         float j2y[4], j2x[4];
 #pragma unroll
-                        for (int q = 0; q < 4; ++q)
+                        for (int q = 0; q < 4; q += 2)
                         {
-                            j2y[q] = fmaf(k.ndy, sxm[2][q] - sxm[0][q], jcy[q]);
-                            j2x[q] = fmaf(k.jx3, dxm[1][q], fmaf(k.jx1, dxm[2][q] + dxm[0][q], jcx[q]));
+                            const auto P = [q](const float (&v)[4]) { return make_float2(v[q], v[q + 1]); };
+                            const float2 vy = __ffma2_rn(k.ndyp, sub2(P(sxm[2]), P(sxm[0])), P(jcy));
+                            const float2 vx = __ffma2_rn(k.jx3p, P(dxm[1]),
+                                                         __ffma2_rn(k.jx1p, __fadd2_rn(P(dxm[2]), P(dxm[0])), P(jcx)));
+                            j2y[q] = vy.x; j2y[q + 1] = vy.y;
+                            j2x[q] = vx.x; j2x[q + 1] = vx.y;
                         }
                         float4 cy4 = lds4(&h[1][4 * lane]), cx4 = lds4(&h[2][4 * lane]);
                         jcy[0] = cy4.x; jcy[1] = cy4.y; jcy[2] = cy4.z; jcy[3] = cy4.w;  // J_c at row kl
@@ -481,9 +509,15 @@ namespace amb
                             dxj[0][q] = dxj[1][q]; dxj[1][q] = dxj[2][q];
                             sxj[2][q] = fmaf(0.1f, yy[q] + yy[q + 2], 0.3f * yy[q + 1]);
                             dxj[2][q] = xx[q + 2] - xx[q];
-                            float v = k.tx1 * (dxj[0][q] + dxj[2][q]);
-                            v = fmaf(k.tx3, dxj[1][q], v);
-                            dtj[q] = fmaf(k.dyInv, sxj[2][q] - sxj[0][q], v);
+                        }
+#pragma unroll
+                        for (int q = 0; q < 4; q += 2)
+                        {
+                            const auto P = [q](const float (&v)[4]) { return make_float2(v[q], v[q + 1]); };
+                            float2 v = __fmul2_rn(k.tx1p, __fadd2_rn(P(dxj[0]), P(dxj[2])));
+                            v = __ffma2_rn(k.tx3p, P(dxj[1]), v);
+                            v = __ffma2_rn(k.dyInvp, sub2(P(sxj[2]), P(sxj[0])), v);
+                            dtj[q] = v.x; dtj[q + 1] = v.y;
                         }
                         sts4(&sm.dtj[(kl - 2) & (kDelay - 1)][4 * lane], dtj);
                     }
@@ -523,7 +557,7 @@ namespace amb
                         __syncwarp();
                         float4 dt4 = lds4(&sm.dtj[lo & (kDelay - 1)][4 * lane]);
                         float4 dy4 = lds4(&h[3][4 * lane]);
-                        float dtv[4] = {dt4.x + dy4.x, dt4.y + dy4.y, dt4.z + dy4.z, dt4.w + dy4.w};
+                        const float dtv[4] = {dt4.x, dt4.y, dt4.z, dt4.w}, dyv[4] = {dy4.x, dy4.y, dy4.z, dy4.w};
                         float4 ph4 = lds4(&sm.phi[lo & (kRing - 1)][own]);
                         float fo[4] = {ph4.x, ph4.y, ph4.z, ph4.w};
                         const size_t gi = (size_t)grow * nx + gcol;
@@ -535,27 +569,38 @@ namespace amb
                             rr[2] = __uint_as_float(rv.y << 16);
                             rr[3] = __uint_as_float(rv.y & 0xffff0000u);
                         }
-                        float nf[4], nr[4];
+                        float dx8[4];
 #pragma unroll
                         for (int q = 0; q < 4; ++q)
                         {
-                            float dx8 = k.px8[0] * (jj[q + 5] - jj[q + 3]);
-                            dx8 = fmaf(k.px8[1], jj[q + 6] - jj[q + 2], dx8);
-                            dx8 = fmaf(k.px8[2], jj[q + 7] - jj[q + 1], dx8);
-                            dx8 = fmaf(k.px8[3], jj[q + 8] - jj[q], dx8);
-                            float div = dx8 + dtv[q];
+                            float d = k.px8[0] * (jj[q + 5] - jj[q + 3]);
+                            d = fmaf(k.px8[1], jj[q + 6] - jj[q + 2], d);
+                            d = fmaf(k.px8[2], jj[q + 7] - jj[q + 1], d);
+                            dx8[q] = fmaf(k.px8[3], jj[q + 8] - jj[q], d);
+                        }
+                        // div = DX8 + (divTj + DY8); compensated update phi += y, y = -dt div - r,
+                        // in column pairs: y = -F with F = fma(dt, div, r) (the same rounding),
+                        // new phi = phi - F, new r = (new phi - phi) + F
+                        float nf[4], nr[4];
+#pragma unroll
+                        for (int q = 0; q < 4; q += 2)
+                        {
+                            const auto P = [q](const float (&v)[4]) { return make_float2(v[q], v[q + 1]); };
+                            const float2 div = __fadd2_rn(P(dx8), __fadd2_rn(P(dtv), P(dyv)));
+                            float2 vf, vr;
                             if constexpr (COMP == COMP_BF16)
                             {
-                                float y = fmaf(-k.dt, div, -rr[q]);
-                                float tt = fo[q] + y;
-                                nr[q] = (tt - fo[q]) - y;
-                                nf[q] = tt;
+                                const float2 F = __ffma2_rn(k.dtp, div, P(rr));
+                                vf = sub2(P(fo), F);
+                                vr = __fadd2_rn(sub2(vf, P(fo)), F);
                             }
                             else
                             {
-                                nf[q] = fmaf(-k.dt, div, fo[q]);
-                                nr[q] = 0.f;
+                                vf = __ffma2_rn(k.ndtp, div, P(fo));
+                                vr = make_float2(0.f, 0.f);
                             }
+                            nf[q] = vf.x; nf[q + 1] = vf.y;
+                            nr[q] = vr.x; nr[q + 1] = vr.y;
                         }
                         if (*reinterpret_cast<volatile int*>(&sm.abort))
                             nf[0] = nf[1] = nf[2] = nf[3] = __int_as_float(0x7fc00000);
@@ -601,8 +646,10 @@ namespace amb
         // Batched form: one warp pair per task of a task table that spans many replicas of
         // different sizes and parameters; the step index comes from device memory so that
         // a captured CUDA graph of several steps can be replayed.
+        // (6 one-pair CTAs per SM: at most 168 registers without spills; the per-replica
+        // coefficients come from a table in global memory, not from kernel parameters)
         template <int COMP, int NOISE>
-        __global__ void __launch_bounds__(64)
+        __global__ void __launch_bounds__(64, 6)
         sliding_ensemble_kernel(const EnsembleReplica* __restrict__ reps, const Coef* __restrict__ coefs,
                                 const EnsembleTask* __restrict__ tasks, int parity,
                                 const int64_t* __restrict__ step_counter, int step_offset)
