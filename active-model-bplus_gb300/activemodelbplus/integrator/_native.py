@@ -100,6 +100,10 @@ SIGNATURES = {
     "amb_learned_spectral_combine_noise": (_I, [_VP, _VP, _VP, _VP, _VP, ctypes.c_double, _I, _I, _I64, _I64, _U64,
                                                 _VP, _VP, _VP, _VP]),
     "amb_learned_noise": (_I, [_I, _I, _U64, _VP, _VP, _VP]),
+    "amb_learned_fft_create": (_I, [_I, _I, ctypes.POINTER(_VP)]),
+    "amb_learned_fft_forward": (_I, [_VP, _VP, _VP, _VP]),
+    "amb_learned_fft_inverse2": (_I, [_VP, _VP, _VP, _VP]),
+    "amb_learned_fft_destroy": (None, [_VP]),
     "amb_learned_update": (_I, [_VP, _VP, _I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, _VP,
                                 ctypes.c_double, _VP, _VP, ctypes.c_double, _VP, _VP, _VP]),
     "amb_learned_update_input": (_I, [_VP, _VP, _I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, _VP,

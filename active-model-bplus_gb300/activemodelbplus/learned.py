@@ -516,6 +516,7 @@ class LinearPart:
         self.nx_ = torch.from_numpy(np.broadcast_to(g * sym_x, full).astype(np.complex64)).to(dev)
         self._layout = None
         self._filters = None
+        self._fft = None
 
     def flux(self, phi):
         """Linear part only: phi [B, H, W] -> G [B, 2, H, W] (component 0 = y face, 1 = x face)."""
@@ -524,6 +525,48 @@ class LinearPart:
         gy = torch.fft.irfft2(spec * self.my, s=self.shape)
         gx = torch.fft.irfft2(spec * self.mx, s=self.shape)
         return torch.stack([gy, gx], dim=1)
+
+    def _extra_direct(self, phi, noise_mag: float, out, spectral_noise):
+        """extra() without a per-site noise field, on the library's own cuFFT plans
+        (``amb_learned_fft_*``): one forward transform, the combining kernel (noise drawn in it
+        when ``spectral_noise`` is given), one batched inverse into ``out``; the spectra live in
+        buffers made on the first call, so later calls can be captured in a CUDA graph."""
+        torch = _torch()
+        lib = N.lib()
+        ny, nx = self.shape
+        nk = nx // 2 + 1
+        if self._fft is None:
+            h = ctypes.c_void_p()
+            _check(lib.amb_learned_fft_create(ny, nx, ctypes.byref(h)))
+            self._fft = h
+            self._spec = torch.empty(ny, nk, dtype=torch.complex64, device=phi.device)
+            self._comb = torch.empty(2, ny, nk, dtype=torch.complex64, device=phi.device)
+            inv_n = 1.0 / (ny * nx)  # the inverse transform is unnormalised
+            self._filters_rm = [(f * inv_n).contiguous() for f in (self.my, self.mx, self.ny_, self.nx_)]
+        if not (phi.is_contiguous() and out.is_contiguous() and phi.dtype == torch.float32
+                and out.dtype == torch.float32 and tuple(out.shape) == (2, ny, nx)):
+            raise ValueError("LinearPart.extra: phi [H, W] and out [2, H, W] must be contiguous float32")
+        _check(lib.amb_learned_fft_forward(self._fft, _ptr(phi), _ptr(self._spec), _stream()))
+        my, mx, nyf, nxf = self._filters_rm
+        if spectral_noise is not None:
+            seed, step = spectral_noise
+            _check(lib.amb_learned_spectral_combine_noise(
+                _ptr(self._spec), _ptr(my), _ptr(mx), _ptr(nyf), _ptr(nxf), float(noise_mag), ny, nx, nk, 1,
+                int(seed), _ptr(step), _ptr(self._comb[0]), _ptr(self._comb[1]), _stream()))
+        else:
+            _check(lib.amb_learned_spectral_combine(
+                _ptr(self._spec), None, _ptr(my), _ptr(mx), _ptr(nyf), _ptr(nxf), 0.0, ny * nk,
+                _ptr(self._comb[0]), _ptr(self._comb[1]), _stream()))
+        _check(lib.amb_learned_fft_inverse2(self._fft, _ptr(self._comb), _ptr(out), _stream()))
+        return out
+
+    def __del__(self):
+        if getattr(self, "_fft", None) is not None:
+            try:
+                N.lib().amb_learned_fft_destroy(self._fft)
+            except Exception:
+                pass
+            self._fft = None
 
     def extra(self, phi, xi, noise_mag: float, out, spectral_noise=None):
         """Linear part of phi [H, W] plus the noise flux of xi [2, H, W] (or None) into out [2, H, W]:
@@ -534,10 +577,12 @@ class LinearPart:
         keyed by the device step counter) instead of transforming xi: statistically the same
         white noise, two forward FFTs and one kernel fewer."""
         torch = _torch()
-        spec = torch.fft.rfft2(phi)
-        sxi = torch.fft.rfft2(xi) if xi is not None else None
-        if not spec.is_cuda:
+        if not phi.is_cuda:
             raise CudaException("LinearPart.extra runs on the GPU")
+        if xi is None:
+            return self._extra_direct(phi, noise_mag, out, spectral_noise)
+        spec = torch.fft.rfft2(phi)
+        sxi = torch.fft.rfft2(xi)
         # cuFFT through torch may return the spectrum in a transposed (column-major) layout: the
         # combining kernel works in memory order, so the filters are kept in the FFT's layout
         # (converted once) and the spectra are used as they come when they are dense in it; a

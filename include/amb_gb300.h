@@ -330,6 +330,17 @@ int amb_learned_spectral_combine(const void* phi_hat, const void* xi_hat, const 
                                  const void* ny, const void* nx, double noise_mag, int64_t n, void* out_y,
                                  void* out_x, void* stream);
 
+/* cuFFT plans for the learned stepper's spectral pass on nrows x ncols fields, created (with
+ * their work areas) by amb_learned_fft_create: amb_learned_fft_forward is the real-to-complex
+ * transform of one field into a row-major [nrows][ncols/2+1] complex64 spectrum;
+ * amb_learned_fft_inverse2 the unnormalised complex-to-real transform of two such spectra
+ * (consecutive, overwritten) into two consecutive fields. Both are stream-ordered and can be
+ * captured in a CUDA graph. */
+int amb_learned_fft_create(int nrows, int ncols, void** handle);
+int amb_learned_fft_forward(void* handle, const float* field, void* spectrum, void* stream);
+int amb_learned_fft_inverse2(void* handle, void* spectra, float* fields, void* stream);
+void amb_learned_fft_destroy(void* handle);
+
 /* amb_learned_spectral_combine with xi_hat drawn in place: the draw amb_learned_noise_spectral
  * makes for the same seed and *step. All spectra are [nrows][ncols/2+1] complex64 in one dense
  * layout given by its strides (row-major: col_stride 1, row_stride ncols/2+1; column-major:

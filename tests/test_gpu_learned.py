@@ -499,3 +499,30 @@ def test_update_writes_the_next_network_input():
     assert s.fallback_spans >= 1
     ref = L.network_input(s.phi_f.unsqueeze(0), s.params)
     assert torch.equal(s._x.view(torch.int16), ref.view(torch.int16))
+
+
+def test_learned_fft_plans_match_torch_fft():
+    """amb_learned_fft_forward equals torch's rfft2; amb_learned_fft_inverse2 is the
+    unnormalised inverse of two spectra at once (FP32 rounding)."""
+    import ctypes
+    torch, L, N = mods()
+    H, W = 96, 256
+    lib = N.lib()
+    h = ctypes.c_void_p()
+    assert lib.amb_learned_fft_create(H, W, ctypes.byref(h)) == 0, N.last_error()
+    try:
+        strm = torch.cuda.current_stream().cuda_stream
+        g = torch.Generator(device="cpu").manual_seed(3)
+        phi = torch.randn(H, W, generator=g).cuda()
+        spec = torch.empty(H, W // 2 + 1, dtype=torch.complex64, device="cuda")
+        assert lib.amb_learned_fft_forward(h, phi.data_ptr(), spec.data_ptr(), strm) == 0
+        ref = torch.fft.rfft2(phi)
+        assert float((spec - ref).abs().max()) < 1e-4 * float(ref.abs().max())
+        two = torch.randn(2, H, W, generator=g).cuda()
+        spectra = torch.fft.rfft2(two).contiguous()
+        out = torch.empty(2, H, W, device="cuda")
+        assert lib.amb_learned_fft_inverse2(h, spectra.data_ptr(), out.data_ptr(), strm) == 0
+        assert float((out / (H * W) - two).abs().max()) < 1e-5
+    finally:
+        lib.amb_learned_fft_destroy(h)
+    assert lib.amb_learned_fft_create(1, W, ctypes.byref(h)) != 0
