@@ -55,6 +55,14 @@ namespace amb
     // published multipliers and Weyl key increments.
     struct U4 { uint32_t x, y, z, w; };
 
+    // One 32 x 32 -> 64-bit product per multiplier (a single wide multiply gives both halves).
+    __device__ __forceinline__ void mulhilo(uint32_t m, uint32_t x, uint32_t& hi, uint32_t& lo)
+    {
+        const uint64_t p = uint64_t(m) * x;
+        hi = uint32_t(p >> 32);
+        lo = uint32_t(p);
+    }
+
     __device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1)
     {
         constexpr uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
@@ -62,8 +70,9 @@ namespace amb
 #pragma unroll
         for (int round = 0; round < 10; ++round)
         {
-            uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
-            uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+            uint32_t hi0, lo0, hi1, lo1;
+            mulhilo(M0, c.x, hi0, lo0);
+            mulhilo(M1, c.z, hi1, lo1);
             c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
             k0 += W0;
             k1 += W1;
@@ -79,8 +88,9 @@ namespace amb
 #pragma unroll
         for (int round = 0; round < 10; ++round)
         {
-            uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
-            uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+            uint32_t hi0, lo0, hi1, lo1;
+            mulhilo(M0, c.x, hi0, lo0);
+            mulhilo(M1, c.z, hi1, lo1);
             c = U4{hi1 ^ c.y ^ rk0[round], lo1, hi0 ^ c.w ^ rk1[round], lo0};
         }
         return c;
