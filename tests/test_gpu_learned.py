@@ -353,22 +353,26 @@ def test_filtered_macro_noise_matches_k_plain_steps():
         p = np.abs(np.fft.fft2(d)).ravel() ** 2
         return np.array([p[bins == b].mean() for b in range(1, 15)])
 
-    sp_plain, sp_f, sp_u = 0, 0, 0
+    sp_plain, sp_f, sp_s, sp_u = 0, 0, 0, 0
     for seed in range(8):
         sim = Integrator(np.ones((H, W)), st, m, precision="f64", seed=100 + seed)
         sim.run(K)
         sp_plain = sp_plain + spectrum(sim.field - 1.0)
-        for filt in (True, False):
+        # filtered noise drawn as a spectrum (default), filtered noise drawn per site, unfiltered
+        for filt, spec in ((True, True), (True, False), (False, True)):
             s = L.LearnedStepper(net, np.ones((H, W)), st, m, K=K, seed=200 + seed, check_every=1, tol=1e9,
-                                 filter_noise=filt, use_graph=False)
+                                 filter_noise=filt, spectral_noise=spec, use_graph=False)
             s.advance(1)
             d = s.field - 1.0
-            if filt:
+            if filt and spec:
                 sp_f = sp_f + spectrum(d)
+            elif filt:
+                sp_s = sp_s + spectrum(d)
             else:
                 sp_u = sp_u + spectrum(d)
-    ratio = sp_f / sp_plain
-    assert np.all(np.abs(ratio - 1) < 0.12), ratio
+    for sp in (sp_f, sp_s):
+        ratio = sp / sp_plain
+        assert np.all(np.abs(ratio - 1) < 0.12), ratio
     assert (sp_u / sp_plain).max() > 3, sp_u / sp_plain
 
 
