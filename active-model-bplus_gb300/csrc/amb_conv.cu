@@ -326,7 +326,9 @@ namespace
 
         if (threadIdx.x == 0)
         {
-            for (int i = 0; i < R + 4; ++i) mbar_init(&full[i], 1);
+            // a row completes with its bulk copies and one arrival per wrapped site (below)
+            const int wrapped = (c0 == 0 ? 2 : 0) + (c0 + kTile == a.ncols ? 2 : 0);
+            for (int i = 0; i < R + 4; ++i) mbar_init(&full[i], 1 + cc * wrapped);
             for (int i = 0; i < R; ++i) mbar_init(&accf[i], 1);
             mbar_init(zbar, 256);
             mbar_init(wbar, 1);
@@ -346,6 +348,14 @@ namespace
 
         if (warp == 0)
         {
+            // The window's sites c0-2 .. c0+129 of each (row, channel chunk): the in-range run by
+            // ONE bulk copy here; where the window wraps round the periodic row (first and last
+            // windows, 2 sites each side) the epilogue warps copy the wrapped 16-byte sites
+            // before their first wait (one mbarrier arrival each).
+            const int left = c0 == 0 ? 2 : 0;
+            const int right = c0 + kTile == a.ncols ? 2 : 0;
+            const int lo = c0 - 2 + left;          // first in-range column of the window
+            const int run = kSites - left - right; // in-range sites
             if (lane == 0)
             {
                 // every input row of this CTA at once, one mbarrier per row, in the order
@@ -355,12 +365,13 @@ namespace
                 for (int i = 0; i < nin; ++i)
                 {
                     const int row = wrap_row(r0 - 2 + i, a.nrows);
-                    mbar_expect_tx(&full[i], slot_bytes);
+                    mbar_expect_tx(&full[i], uint32_t(cc * run) * 16u);
                     uint8_t* dst = rows + i * slot_bytes;
                     for (int q = 0; q < cc; ++q)
                     {
                         const uint16_t* src = a.in + (size_t(b * cc + q) * a.nrows + row) * size_t(a.ncols) * 8;
-                        stage_window(dst + q * kRowPlane, src, c0, a.ncols, &full[i]);
+                        bulk_g2s(dst + q * kRowPlane + left * 16, src + size_t(lo) * 8, uint32_t(run) * 16u,
+                                 &full[i]);
                     }
                 }
                 // no copy may still be in flight when the CTA exits
@@ -439,6 +450,27 @@ namespace
             tmem_wait_st();
             tc_fence_before();
             mbar_arrive(zbar);
+            {
+                // the wrapped sites of the staged rows (see warp 0): 16-byte plain copies, made
+                // visible to the async proxy, one arrival on the row's mbarrier each
+                const int left = c0 == 0 ? 2 : 0;
+                const int right = c0 + kTile == a.ncols ? 2 : 0;
+                const int per_chunk = left + right, per_row = cc * per_chunk;
+                for (int it = int(threadIdx.x) - 64; it < nin * per_row; it += kFwdThreads - 64)
+                {
+                    const int i = it / per_row, rem = it - i * per_row;
+                    const int q = rem / per_chunk, s = rem - q * per_chunk;
+                    const bool at_left = s < left;
+                    const int wsite = at_left ? s : kSites - right + (s - left);  // site in the window
+                    const int gcol = at_left ? a.ncols - 2 + s : s - left;        // its periodic column
+                    const int row = wrap_row(r0 - 2 + i, a.nrows);
+                    const uint4 v = *reinterpret_cast<const uint4*>(
+                        a.in + ((size_t(b * cc + q) * a.nrows + row) * size_t(a.ncols) + gcol) * 8);
+                    *reinterpret_cast<uint4*>(rows + i * slot_bytes + q * kRowPlane + wsite * 16) = v;
+                    fence_proxy_async();
+                    mbar_arrive(&full[i]);
+                }
+            }
             for (int j = 0; j < nout; ++j)
             {
                 bool ok = mbar_wait(&accf[j], 0, abort);

@@ -205,3 +205,28 @@ def test_spectral_noise_flux_equals_face_sums_of_the_filtered_draw():
     fx = sum(w[i] * np.roll(shaped[1], -e, axis=1) for i, e in enumerate(range(-3, 5))) * 3.0
     assert np.abs(out[0].numpy() - fy).max() < 1e-4
     assert np.abs(out[1].numpy() - fx).max() < 1e-4
+
+
+def test_forward_staging_covers_each_window_once():
+    """The forward convolution stages each 132-site window (columns c0-2 .. c0+129, periodic)
+    as one in-range bulk copy plus per-site copies of the wrapped sites: an emulation of that
+    index arithmetic (csrc/amb_conv.cu, conv_fwd_kernel, warp 0) reproduces the periodic window
+    exactly, writes every window site once and reads only columns of the row."""
+    k_tile, k_sites = 128, 132
+    for ncols in (128, 256, 512, 1024):
+        for c0 in range(0, ncols, k_tile):
+            left = 2 if c0 == 0 else 0
+            right = 2 if c0 + k_tile == ncols else 0
+            lo, run = c0 - 2 + left, k_sites - left - right
+            window = [None] * k_sites
+            assert 0 <= lo and lo + run <= ncols
+            for s in range(run):  # the bulk copy
+                assert window[left + s] is None
+                window[left + s] = lo + s
+            for s in range(left + right):  # the wrapped sites
+                at_left = s < left
+                wsite = s if at_left else k_sites - right + (s - left)
+                gcol = ncols - 2 + s if at_left else s - left
+                assert 0 <= gcol < ncols and window[wsite] is None
+                window[wsite] = gcol
+            assert window == [(c0 - 2 + j) % ncols for j in range(k_sites)], (ncols, c0)
