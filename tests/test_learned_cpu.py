@@ -230,3 +230,26 @@ def test_forward_staging_covers_each_window_once():
                 assert 0 <= gcol < ncols and window[wsite] is None
                 window[wsite] = gcol
             assert window == [(c0 - 2 + j) % ncols for j in range(k_sites)], (ncols, c0)
+
+
+def test_spectral_combine_noise_index_map():
+    """spectral_combine_noise_kernel recovers each rfft2 mode (r, k) from its memory index i for
+    a row-major (ks = 1, rs = W/2+1) or column-major (rs = 1, ks = H) spectrum (csrc/amb_conv.cu):
+    an emulation visits every mode exactly once, and the Hermitian partner used for the k = 0
+    and Nyquist columns (r -> H - r above H/2) stays a valid row."""
+    for H, W in ((8, 16), (6, 10), (5, 8), (96, 128)):
+        nk = W // 2 + 1
+        for rs, ks in ((nk, 1), (1, H)):
+            seen = set()
+            for i in range(H * nk):
+                if ks == 1:
+                    r, k = i // rs, i - (i // rs) * rs
+                else:
+                    k, r = i // ks, i - (i // ks) * ks
+                assert 0 <= r < H and 0 <= k < nk
+                assert r * rs + k * ks == i
+                seen.add((r, k))
+                herm = k == 0 or (W % 2 == 0 and k == W // 2)
+                if herm and r > H // 2:
+                    assert 0 < H - r < H
+            assert len(seen) == H * nk
