@@ -10,8 +10,10 @@
 //
 // Forward / data-gradient kernel (conv_fwd_kernel): one CTA owns a 128-site
 // window of up to 16 output rows and stages all of its input rows (the rows plus
-// a 2-row halo above and below, periodic wrap in both axes) in shared memory with
-// bulk copies, one mbarrier per row. Each staged input row, shifted by one of the
+// a 2-row halo above and below, periodic wrap in both axes) in shared memory, one
+// bulk copy per (row, channel chunk) for the in-range sites and, in the first and
+// last windows, plain copies of the 2 periodically wrapped sites on each side by
+// the epilogue warps; one mbarrier per row. Each staged input row, shifted by one of the
 // five x taps, is the A operand (M = 128 sites, K-major, LBO = one channel-chunk
 // plane, SBO = 8 sites) of ONE MMA per 16 input channels whose B operand stacks
 // the five y taps along N (N = 5 x Cout): its five N slices are the contributions
@@ -135,23 +137,6 @@ namespace
     {
         r %= n;
         return r < 0 ? r + n : r;
-    }
-
-    // Stages the kSites = 132 sites (c0 - 2 .. c0 + 129, periodic in the row) of one channel
-    // chunk of one row into dst as contiguous runs: one bulk copy when the window does not wrap,
-    // at most three when it does (rows of 128 sites wrap on both sides).
-    __device__ __forceinline__ void stage_window(uint8_t* dst, const uint16_t* row_src, int c0, int ncols,
-                                                 uint64_t* bar)
-    {
-        int cur = c0 - 2 < 0 ? c0 - 2 + ncols : c0 - 2;
-        int done = 0;
-        while (done < kSites)
-        {
-            const int len = min(kSites - done, ncols - cur);
-            bulk_g2s(dst + done * 16, row_src + size_t(cur) * 8, uint32_t(len) * 16u, bar);
-            done += len;
-            cur = 0;
-        }
     }
 
     // GELU in its tanh form (Hendrycks and Gimpel): 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))),
@@ -574,9 +559,12 @@ namespace
         const int nx_rows = nout + wg_extra_rows(cc);
         const int kb = wg_kb(cc), nst = wg_nstarts(cc);
 
+        // the X windows' wrapped sites (first and last windows) are copied by the epilogue
+        // warps, one arrival on `ld` each (see the forward kernel)
+        const int wleft = c0 == 0 ? 2 : 0, wright = c0 + kTile == a.ncols ? 2 : 0;
         if (threadIdx.x == 0)
         {
-            mbar_init(ld, 1);
+            mbar_init(ld, 1 + nx_rows * cc * (wleft + wright));
             mbar_init(done, 1);
             *abort = 0;
             fence_mbar_init();
@@ -595,7 +583,8 @@ namespace
         {
             if (lane == 0)
             {
-                const uint32_t bytes = uint32_t(nx_rows) * xrow + uint32_t(nout) * dzrow;
+                const int lo = c0 - 2 + wleft, run = kSites - wleft - wright;  // in-range run of a window
+                const uint32_t bytes = uint32_t(nx_rows * cc * run) * 16u + uint32_t(nout) * dzrow;
                 mbar_expect_tx(ld, bytes);
                 for (int i = 0; i < nx_rows; ++i)
                 {
@@ -603,7 +592,8 @@ namespace
                     for (int q = 0; q < cc; ++q)
                     {
                         const uint16_t* src = a.x + (size_t(b * cc + q) * a.nrows + row) * size_t(a.ncols) * 8;
-                        stage_window(xs + i * xrow + q * kRowPlane, src, c0, a.ncols, ld);
+                        bulk_g2s(xs + i * xrow + q * kRowPlane + wleft * 16, src + size_t(lo) * 8,
+                                 uint32_t(run) * 16u, ld);
                     }
                 }
                 for (int j = 0; j < nout; ++j)
@@ -651,6 +641,23 @@ namespace
             const int g = m >> 3, e = m & 7;
             const int kyb = g / cc, ci = (g % cc) * 8 + e;
             const int cin = cc * 8;
+            {
+                const int per_chunk = wleft + wright, per_row = cc * per_chunk;
+                for (int it = int(threadIdx.x) - 64; it < nx_rows * per_row; it += kThreads - 64)
+                {
+                    const int i = it / per_row, rem = it - i * per_row;
+                    const int q = rem / per_chunk, s = rem - q * per_chunk;
+                    const bool at_left = s < wleft;
+                    const int wsite = at_left ? s : kSites - wright + (s - wleft);
+                    const int gcol = at_left ? a.ncols - 2 + s : s - wleft;
+                    const int row = wrap_row(r0 - 2 + i, a.nrows);
+                    const uint4 v = *reinterpret_cast<const uint4*>(
+                        a.x + ((size_t(b * cc + q) * a.nrows + row) * size_t(a.ncols) + gcol) * 8);
+                    *reinterpret_cast<uint4*>(xs + i * xrow + q * kRowPlane + wsite * 16) = v;
+                    fence_proxy_async();
+                    mbar_arrive(ld);
+                }
+            }
             bool ok = mbar_wait(done, 0, abort);
             ok = __all_sync(0xffffffffu, ok);
             if (ok)
