@@ -14,12 +14,14 @@ weights and activations with FP32 accumulation; its forward and both backward
 passes run on this package's own tcgen05 implicit-GEMM kernels
 (``amb_conv5x5_forward`` / ``amb_conv5x5_wgrad``). Training targets are the
 deterministic K-step increments of the plain integrator started from states of
-noisy trajectories; the noise of a macro step is one Philox draw shaped per Fourier
-mode by the K-step accumulation of the linearised plain scheme (``noise_filter``). The plain integrator is the
-fallback: every ``check_every`` macro steps one step is compared with K plain
-deterministic steps from the same state, and if the residual exceeds ``tol``
-(or the field left its bounds) the span since the last check is redone with
-the plain integrator.
+noisy trajectories; the noise of a macro step is one Philox draw, made directly
+as its Fourier spectrum and shaped per mode by the K-step accumulation of the
+linearised plain scheme (``noise_filter``). The plain integrator is the fallback:
+at the end of each span of macro steps one step is compared with K plain
+deterministic steps from the same state, and if the residual exceeds ``tol`` (or
+the field left its bounds) the span is redone with the plain integrator. Spans
+start at ``check_every`` macro steps and double, up to ``max_check_every``, while
+the residuals stay below tol/4.
 """
 from __future__ import annotations
 
