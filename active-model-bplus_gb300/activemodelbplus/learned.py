@@ -831,11 +831,8 @@ class LearnedStepper:
             if ok:
                 self._macro_step()
                 ok = int(self.flag.item()) == 0
-            res = self.residuals[-1]
-            if ok and res < 0.25 * self.tol:
-                self.interval = min(2 * self.interval, self.max_check_every)
-            elif not ok or res > 0.5 * self.tol:
-                self.interval = self.check_every
+            self.interval = next_check_interval(self.interval, self.residuals[-1], ok, self.tol, self.check_every,
+                                                self.max_check_every)
             if ok:
                 self.learned_steps += span
             else:
@@ -854,6 +851,17 @@ class LearnedStepper:
         if not math.isclose(n * self.dtk, t, rel_tol=1e-9, abs_tol=1e-12):
             raise ValueError(f"t={t} is not a multiple of K dt = {self.dtk}")
         self.advance(n)
+
+
+def next_check_interval(interval: int, residual: float, accepted: bool, tol: float, base: int, longest: int) -> int:
+    """Macro steps until the next residual check: doubled (up to ``longest``) after an accepted
+    check whose residual is below tol/4, back to ``base`` after a residual above tol/2 or a
+    failed check, unchanged otherwise."""
+    if accepted and residual < 0.25 * tol:
+        return min(2 * interval, longest)
+    if not accepted or not residual <= 0.5 * tol:
+        return base
+    return interval
 
 
 def torch_round_fix(f):

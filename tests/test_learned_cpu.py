@@ -253,3 +253,20 @@ def test_spectral_combine_noise_index_map():
                 if herm and r > H // 2:
                     assert 0 < H - r < H
             assert len(seen) == H * nk
+
+
+def test_adaptive_check_interval_rules():
+    """The learned stepper's check cadence: doubles to the cap while residuals stay below tol/4,
+    holds between tol/4 and tol/2, resets after a larger residual, a NaN or a failed check."""
+    from activemodelbplus.learned import next_check_interval as nxt
+    tol, base, cap = 0.5, 40, 320
+    seq, iv = [], base
+    for _ in range(5):
+        iv = nxt(iv, 0.04, True, tol, base, cap)
+        seq.append(iv)
+    assert seq == [80, 160, 320, 320, 320]
+    assert nxt(160, 0.2, True, tol, base, cap) == 160          # between tol/4 and tol/2: hold
+    assert nxt(160, 0.3, True, tol, base, cap) == base         # above tol/2: reset
+    assert nxt(160, 0.01, False, tol, base, cap) == base       # failed check: reset
+    assert nxt(160, float("nan"), True, tol, base, cap) == base
+    assert nxt(40, 0.0, True, tol, 40, 40) == 40               # fixed cadence when the cap is the base
