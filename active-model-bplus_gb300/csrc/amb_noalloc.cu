@@ -158,9 +158,18 @@ extern "C" int amb_mass_f32_noalloc(const float* field, int64_t n, double* out_s
     if (int rc = scratch_on_current_device(&scratch)) return rc;
     const int parts = int((n + kChunk - 1) / kChunk);
     auto s = static_cast<cudaStream_t>(stream);
+    // An error left pending by an earlier, unrelated call is not this call's: it is reported
+    // without being cleared, so the caller's own error check still sees it.
+    const cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess)
+    {
+        amb::set_last_error(std::string("amb_mass_f32_noalloc: an earlier CUDA error is pending: ")
+                            + cudaGetErrorString(pending));
+        return AMB_ERR_CUDA;
+    }
     chunk_sum_kernel<<<parts, kBlock, 0, s>>>(field, n, scratch);
     fold_kernel<<<1, kBlock, 0, s>>>(scratch, parts, out_sum);
-    cudaError_t e = cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();  // nothing was pending, so this is a launch error of ours
     if (e != cudaSuccess)
     {
         amb::set_last_error(std::string("amb_mass_f32_noalloc: ") + cudaGetErrorString(e));

@@ -16,11 +16,12 @@ Keys beyond the base contract:
                float64 host buffers: set_field + run(inner) + get_field per step.
   roofline     step kernel: 8 B x sites per launch / CUDA-event launch time,
                against MEASURED_PEAKS.json hbm_gbs.
-  cpu_baseline the oracle port (C, OpenMP) on the host cores, bounded sample.
+  cpu_baseline the reference's CPU scheme (test/tjhung_ambplus.h compiled on the
+               host, serial) on a bounded sample; the OpenMP oracle port beside it.
   clocks       nvidia-smi samples during the timed region.
 
 ``--impl reference`` times the reference's CPU implementation of the step
-(oracle/_ref where it loads, else the oracle port) on all host threads.
+(test/tjhung_ambplus.h compiled into oracle/_ref; the oracle port where it is not built).
 """
 from __future__ import annotations
 
@@ -184,36 +185,69 @@ def measured_traffic(args):
     return d.get(key)
 
 
-def cpu_baseline(w, seconds: float = 10.0, use_reference: bool = True):
-    """Time the CPU implementation of the same step on the host cores (bounded sample)."""
-    import oracle
-    field = initial_field(w)
-    threads = os.cpu_count() or 1
-    ref = oracle.reference_lib(fast=True) if use_reference else None
-    p = oracle.Params(dt=w["dt"], dx=w["dx"], dy=w["dy"], a=w["a"], b=w["b"], c=w["c"], kappa=w["kappa"],
-                      lamb=w["lamb"], zeta=w["zeta"], T=w["T"])
-    if ref is not None and w["b"] == 0 and w["a"] == -w["c"]:
-        kind, cores = "reference", 1
-
-        def run(n):
-            return oracle.tjhung_run(field, n, w["dt"], w["dx"], w["c"], w["kappa"], w["lamb"], w["zeta"], fast=True)
-        desc = "test/tjhung_ambplus.h (-Ofast, serial; noise off: its drand48 noise cannot be keyed)"
-    else:
-        kind, cores = "port", threads
-
-        def run(n):
-            return oracle.run(field, p, n, noise="philox" if w["T"] else "none", seed=1, nthreads=threads)
-        desc = "oracle/amb_oracle.c (OpenMP) with Philox noise"
+def _timed_sample(run, sites: int, seconds: float):
+    """Steps of ``run(n)`` sized to take about ``seconds``; returns (steps, wall seconds)."""
     t0 = time.perf_counter()
     run(1)
     t1 = time.perf_counter() - t0
     nsteps = int(max(1, min(200, round(seconds / max(t1, 1e-6)))))
     t0 = time.perf_counter()
     run(nsteps)
-    dt = time.perf_counter() - t0
+    return nsteps, time.perf_counter() - t0
+
+
+def _params(w):
+    import oracle
+    return oracle.Params(dt=w["dt"], dx=w["dx"], dy=w["dy"], a=w["a"], b=w["b"], c=w["c"], kappa=w["kappa"],
+                         lamb=w["lamb"], zeta=w["zeta"], T=w["T"])
+
+
+def cpu_reference_runner(w):
+    """The reference's own CPU scheme (test/tjhung_ambplus.h, -Ofast, serial, with its drand48
+    noise at D = T) on this workload, as ``run(nsteps)``; None where it is not built or the
+    workload is outside the scheme (it needs b = 0, a = -c, dx = dy)."""
+    import oracle
+    if oracle.reference_lib(fast=True) is None or w["b"] != 0 or w["a"] != -w["c"] or w["dx"] != w["dy"]:
+        return None
+    field = initial_field(w)
+
+    def run(n):
+        return oracle.tjhung_run_noisy(field, n, w["dt"], w["dx"], w["c"], w["kappa"], w["lamb"], w["zeta"],
+                                       w["T"], seed=1, fast=True)
+    return run
+
+
+def cpu_port_runner(w, threads: int):
+    """The oracle port (oracle/amb_oracle.c, OpenMP over ``threads``) with Philox noise, as ``run(nsteps)``."""
+    import oracle
+    field = initial_field(w)
+    p = _params(w)
+
+    def run(n):
+        return oracle.run(field, p, n, noise="philox" if w["T"] else "none", seed=1, nthreads=threads)
+    return run
+
+
+def cpu_baseline(w, seconds: float = 10.0):
+    """Time the reference's CPU scheme on the same workload on the host (bounded sample, serial
+    like the scheme itself); the OpenMP oracle port on all host cores is reported beside it."""
     sites = w["ny"] * w["nx"]
-    return {"value": nsteps * sites / dt / 1e9, "unit": UNIT, "cores": cores, "kind": kind,
-            "sample": f"{nsteps} Euler steps of the {w['ny']}x{w['nx']} workload ({dt:.1f} s); {desc}"}
+    threads = os.cpu_count() or 1
+    out = None
+    ref = cpu_reference_runner(w)
+    if ref is not None:
+        n, dt = _timed_sample(ref, sites, seconds)
+        out = {"value": n * sites / dt / 1e9, "unit": UNIT, "cores": 1, "kind": "reference",
+               "sample": f"{n} Euler steps of the {w['ny']}x{w['nx']} workload ({dt:.1f} s); "
+                         f"test/tjhung_ambplus.h compiled -Ofast on this host, serial, its own drand48 noise"}
+    n, dt = _timed_sample(cpu_port_runner(w, threads), sites, seconds)
+    port = {"value": n * sites / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} Euler steps of the {w['ny']}x{w['nx']} workload ({dt:.1f} s); "
+                      f"oracle/amb_oracle.c (OpenMP) with Philox noise"}
+    if out is None:
+        return port
+    out["port"] = port
+    return out
 
 
 def reference_gpu_baseline(w, nsteps: int = 20):
@@ -239,29 +273,25 @@ def reference_gpu_baseline(w, nsteps: int = 20):
 # ------------------------------------------------------------------ arms
 
 def run_reference_arm(args, w, rank, world):
+    """The reference's CPU implementation of the step: test/tjhung_ambplus.h compiled on this host
+    (serial: the scheme is single-threaded and keeps its noise generator in global state), or the
+    OpenMP oracle port on all host threads where the scheme is not built. Each step is one Euler
+    step of the bench workload."""
     if rank != 0:
         return
-    import oracle
-    field = initial_field(w)
     threads = os.cpu_count() or 1
-    p = oracle.Params(dt=w["dt"], dx=w["dx"], dy=w["dy"], a=w["a"], b=w["b"], c=w["c"], kappa=w["kappa"],
-                      lamb=w["lamb"], zeta=w["zeta"], T=w["T"])
-    ref = oracle.reference_lib(fast=True)
+    ref = cpu_reference_runner(w)
     if ref is not None:
-        kind, cores, desc = "reference", 1, "test/tjhung_ambplus.h -Ofast serial, noise off"
-
-        def step():
-            oracle.tjhung_run(field, 1, w["dt"], w["dx"], w["c"], w["kappa"], w["lamb"], w["zeta"], fast=True)
+        kind, cores, desc = "reference", 1, "test/tjhung_ambplus.h -Ofast, serial, its own drand48 noise"
+        run = ref
     else:
         kind, cores, desc = "port", threads, "oracle/amb_oracle.c, OpenMP, Philox noise"
-
-        def step():
-            oracle.run(field, p, 1, noise="philox" if w["T"] else "none", seed=1, nthreads=threads)
+        run = cpu_port_runner(w, threads)
     for _ in range(args.warmup):
-        step()
+        run(1)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        step()
+        run(1)
     dt = time.perf_counter() - t0
     sites = w["ny"] * w["nx"]
     value = args.steps * sites / dt / 1e9

@@ -190,8 +190,11 @@ int amb_mass_f32(const float* field, int64_t n, double* out_sum, void* scratch, 
  * only receive device pointers, or they cannot afford cudaMalloc's synchronization).
  * Scratch is a file-scope device array (256 KiB per GPU, held until process exit);
  * fields above 2^30 sites are rejected with AMB_ERR_INVALID. The first call on each
- * device looks up the array's address and should precede any stream capture. All
- * calls share the array: calls that overlap on the GPU race. */
+ * device looks up the array's address and should precede any stream capture; the address
+ * is cached per device ordinal for the life of the process, so it is stale after a
+ * cudaDeviceReset of that device. All calls share the array: calls that overlap on the
+ * GPU race. An error already pending from an earlier CUDA call is reported (AMB_ERR_CUDA)
+ * and left pending; nothing is launched then. */
 int amb_mass_f32_noalloc(const float* field, int64_t n, double* out_sum, void* stream);
 
 /* ORs 1 into *flag (device int) when any element of the field is NaN or Inf

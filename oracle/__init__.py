@@ -159,8 +159,10 @@ def reference_lib(fast: bool = False):
     key = "fast" if fast else "exact"
     if key not in _ref:
         path = _build.TJHUNG_FAST_LIB if fast else _build.TJHUNG_LIB
-        if _build.reference_available():
-            _build.build_reference()
+        try:
+            _build.build_reference()  # from the staged reference sources, where they exist
+        except RuntimeError:
+            pass
         L = None
         if os.path.exists(path):
             try:
@@ -170,6 +172,8 @@ def reference_lib(fast: bool = False):
         if L is not None:
             L.tjhung_ref_dphi.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 6 + [_DP] * 8
             L.tjhung_ref_run.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 6 + [_DP, ctypes.c_int]
+            L.tjhung_ref_run_noisy.argtypes = ([ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 7
+                                               + [_DP, ctypes.c_int, ctypes.c_long])
         _ref[key] = L
     return _ref[key]
 
@@ -199,6 +203,21 @@ def tjhung_run(phi, nsteps: int, dt: float, h: float, A: float, K: float, lamb: 
     rc = L.tjhung_ref_run(ny, nx, dt, h, A, K, lamb, zeta, _ptr(phi), nsteps)
     if rc:
         raise ValueError("tjhung_ref_run rejected the arguments")
+    return phi
+
+
+def tjhung_run_noisy(phi, nsteps: int, dt: float, h: float, A: float, K: float, lamb: float, zeta: float,
+                     D: float, seed: int = 1, fast: bool = True) -> np.ndarray:
+    """TjhungIntegrator::run with its own noise (D = T; drand48 seeded with ``seed``). No test can
+    pin this noise; it serves the timed CPU baseline, which must run the scheme as it ships."""
+    L = reference_lib(fast)
+    if L is None:
+        raise RuntimeError("reference CPU scheme not built here")
+    phi = _f64(phi).copy()
+    ny, nx = phi.shape
+    rc = L.tjhung_ref_run_noisy(ny, nx, dt, h, A, K, lamb, zeta, D, _ptr(phi), nsteps, seed)
+    if rc:
+        raise ValueError("tjhung_ref_run_noisy rejected the arguments")
     return phi
 
 

@@ -3,12 +3,19 @@
 * ``oracle/_build/libamb_oracle.so`` — the C restatement (``amb_oracle.c``),
   IEEE double arithmetic (no fast-math), optional OpenMP.
 * ``oracle/_ref/libtjhung_ref.so`` and ``libtjhung_ref_fast.so`` — the
-  reference's own CPU scheme ``test/tjhung_ambplus.h`` compiled from the
-  read-only reference checkout through ``tjhung_ref_driver.cc`` with the
-  self-written Eigen stand-in. ``-O2`` for parity pins; ``-Ofast`` (the
-  reference's CMAKE_CXX_FLAGS, CMakeLists.txt:21) for the timed CPU baseline.
-  Built only where the reference checkout exists; elsewhere the prebuilt
-  files (if any) are used as they are.
+  reference's own CPU scheme ``test/tjhung_ambplus.h`` compiled through
+  ``tjhung_ref_driver.cc`` with the self-written Eigen stand-in. ``-O2`` for
+  parity pins; ``-Ofast`` (the reference's CMAKE_CXX_FLAGS, CMakeLists.txt:21)
+  for the timed CPU baseline.
+
+The reference checkout is found through ``AMB_REFERENCE_ROOT`` or, failing
+that, as the directory ``reference`` beside the repository. Where it exists,
+the two reference files the CPU scheme needs (``test/tjhung_ambplus.h`` and
+``src/math_primitives.h``) are staged unmodified into ``oracle/_ref/src/``
+(git-ignored, like every other file under ``oracle/_ref``) and compiled from
+there, so a machine without the checkout (a GPU host of another architecture)
+compiles the same scheme natively from the staged copy. Nothing under
+``oracle/_ref`` is committed.
 """
 from __future__ import annotations
 
@@ -19,7 +26,10 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = os.environ.get("AMB_REFERENCE_ROOT", "/root/reference")
+REPO_ROOT = os.path.dirname(HERE)
+REFERENCE_ROOT = os.environ.get("AMB_REFERENCE_ROOT") or os.path.join(os.path.dirname(REPO_ROOT), "reference")
+STAGED_SRC = os.path.join(REF_DIR, "src")  # staged copy of the reference files the CPU scheme needs
+STAGED_FILES = (os.path.join("test", "tjhung_ambplus.h"), os.path.join("src", "math_primitives.h"))
 
 ORACLE_LIB = os.path.join(BUILD_DIR, "libamb_oracle.so")
 REF_GPU_DRIVER = os.path.join(BUILD_DIR, "libref_gpu_driver.so")
@@ -57,20 +67,46 @@ def reference_available() -> bool:
     return os.path.exists(os.path.join(REFERENCE_ROOT, "test", "tjhung_ambplus.h"))
 
 
+def stage_reference_sources() -> bool:
+    """Copy the reference files the CPU scheme needs into oracle/_ref/src (unmodified).
+    Returns whether a staged copy exists afterwards."""
+    if reference_available():
+        import shutil
+        for rel in STAGED_FILES:
+            src, dst = os.path.join(REFERENCE_ROOT, rel), os.path.join(STAGED_SRC, rel)
+            if not os.path.exists(dst) or os.path.getmtime(src) > os.path.getmtime(dst):
+                os.makedirs(os.path.dirname(dst), exist_ok=True)
+                shutil.copy2(src, dst)
+    return all(os.path.exists(os.path.join(STAGED_SRC, rel)) for rel in STAGED_FILES)
+
+
+def _loads(lib: str) -> bool:
+    """Whether a built library loads on this machine (a copy built for another architecture does not)."""
+    import ctypes
+    try:
+        ctypes.CDLL(lib)
+        return True
+    except OSError:
+        return False
+
+
 def build_reference(force: bool = False) -> list[str]:
-    """Compile the reference's CPU scheme into oracle/_ref (only where the checkout exists)."""
-    if not reference_available():
+    """Compile the reference's CPU scheme into oracle/_ref from the staged sources (staged here
+    from the reference checkout where it exists; on other machines the staged copy that came
+    with the repository copy is compiled natively)."""
+    if not stage_reference_sources():
         return []
     os.makedirs(REF_DIR, exist_ok=True)
     driver = os.path.join(HERE, "tjhung_ref_driver.cc")
     standin = os.path.join(HERE, "eigen_standin")
-    header = os.path.join(REFERENCE_ROOT, "test", "tjhung_ambplus.h")
+    header = os.path.join(STAGED_SRC, "test", "tjhung_ambplus.h")
     built = []
     for lib, opt in ((TJHUNG_LIB, ["-O2", "-ffp-contract=off"]), (TJHUNG_FAST_LIB, ["-Ofast"])):
-        if force or _stale(lib, [driver, header, os.path.join(standin, "Eigen", "Eigen"), __file__]):
+        if force or _stale(lib, [driver, header, os.path.join(standin, "Eigen", "Eigen"), __file__]) \
+                or not _loads(lib):
             tmp = lib + f".tmp{os.getpid()}"
             _run(["g++", "-std=c++20", *opt, "-fPIC", "-shared",
-                  "-I", os.path.join(REFERENCE_ROOT, "test"), "-I", os.path.join(REFERENCE_ROOT, "src"),
+                  "-I", os.path.join(STAGED_SRC, "test"), "-I", os.path.join(STAGED_SRC, "src"),
                   "-I", standin, driver, "-o", tmp])
             os.replace(tmp, lib)
         built.append(lib)
