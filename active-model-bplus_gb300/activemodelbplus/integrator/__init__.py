@@ -179,9 +179,9 @@ class Integrator:
         kernel: "auto", "tile" or "sliding" (FP32 kernel choice).
         autotune: with kernel="auto" and FP32 storage, time the candidate kernels and
             launch shapes for this grid once per process (``amb_autotune_f32``) and use
-            the fastest; otherwise a shape heuristic decides. The two FP32 kernels agree
-            to FP32 rounding, not bitwise; name a kernel for bitwise reproducibility
-            across processes.
+            the fastest; otherwise a shape heuristic decides. The FP32 kernels give
+            bitwise equal fields (the same arithmetic at every site), so the choice
+            changes the time, never the result.
         launch: explicit launch shape of the sliding kernel, {"seg_rows": h, "pairs_per_cta": p}
             (FP32 storage with kernel="sliding"; e.g. a configuration the autotuner reported).
     """
@@ -227,7 +227,7 @@ class Integrator:
         if launch is not None:
             if precision == "f64" or kernel != "sliding":
                 raise ValueError('launch= applies to FP32 storage with kernel="sliding"')
-            self._launch_cfg = N.amb_kernel_config(N.AMB_KERNEL_SLIDING, int(launch.get("seg_rows", 0)),
+            self._launch_cfg = N.amb_kernel_config(_KERNELS[kernel], int(launch.get("seg_rows", 0)),
                                                    int(launch.get("pairs_per_cta", 0)), 0)
         self._tuned = None
         if autotune and kernel == "auto" and precision != "f64":

@@ -22,7 +22,8 @@ OBJ_DIR = os.path.join(PKG_ROOT, "_build")
 LIB_PATH = os.path.join(PKG_ROOT, "activemodelbplus", "integrator", "libamb_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills",
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "-Xptxas", "-warn-spills",
               "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE]
 
 

@@ -21,7 +21,7 @@ namespace amb
                 configured = true;
             }
             dim3 grid((p.nx + TX - 1) / TX, (p.ny + TY - 1) / TY);
-            kern<<<grid, 256, smem, stream>>>(phi_in, phi_out, comp, comp, p, noise_mode, injected);
+            kern<<<grid, 256, smem, stream>>>(phi_in, phi_out, comp, comp, p, Canon<Real>(p), noise_mode, injected);
             return cudaGetLastError();
         }
     }

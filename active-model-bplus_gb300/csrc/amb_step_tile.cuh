@@ -13,6 +13,7 @@
 // register-sliding kernel in amb_step_f32.cu.
 #pragma once
 
+#include "amb_canon.cuh"
 #include "amb_common.cuh"
 #include <cuda_bf16.h>
 
@@ -41,91 +42,11 @@ namespace amb
         }
     };
 
-    template <typename Real>
-    struct Coefs
-    {
-        Real dt, dxInv, dyInv, ex, ey, a, b, c, kappa, lambda, zeta, mag;
-        __device__ __forceinline__ explicit Coefs(const StepParams& p)
-            : dt(Real(p.dt)), dxInv(Real(p.dxInv)), dyInv(Real(p.dyInv)),
-              ex(Real(p.dxInv * p.dxInv)), ey(Real(p.dyInv * p.dyInv)),
-              a(Real(p.a)), b(Real(p.b)), c(Real(p.c)), kappa(Real(p.kappa)),
-              lambda(Real(p.lambda)), zeta(Real(p.zeta)), mag(Real(p.noise_mag)) {}
-    };
-
-    // Tjhung first derivative along x of a row-major array at (i, j), unscaled.
-    template <typename Real>
-    __device__ __forceinline__ Real tj_x(const Real* f, int ld, int i, int j)
-    {
-        const Real* u = f + (i - 1) * ld + j;
-        const Real* m = f + i * ld + j;
-        const Real* d = f + (i + 1) * ld + j;
-        return Real(0.1) * ((u[1] - u[-1]) + (d[1] - d[-1])) + Real(0.3) * (m[1] - m[-1]);
-    }
-
-    template <typename Real>
-    __device__ __forceinline__ Real tj_y(const Real* f, int ld, int i, int j)
-    {
-        const Real* u = f + (i - 1) * ld + j;
-        const Real* d = f + (i + 1) * ld + j;
-        return Real(0.1) * ((d[-1] - u[-1]) + (d[1] - u[1])) + Real(0.3) * (d[0] - u[0]);
-    }
-
-    template <typename Real>
-    __device__ __forceinline__ Real d8_x(const Real* f, int ld, int i, int j)
-    {
-        const Real* m = f + i * ld + j;
-        return Real(d8_tap(1)) * (m[1] - m[-1]) + Real(d8_tap(2)) * (m[2] - m[-2])
-             + Real(d8_tap(3)) * (m[3] - m[-3]) + Real(d8_tap(4)) * (m[4] - m[-4]);
-    }
-
-    template <typename Real>
-    __device__ __forceinline__ Real d8_y(const Real* f, int ld, int i, int j)
-    {
-        const Real* m = f + i * ld + j;
-        return Real(d8_tap(1)) * (m[ld] - m[-ld]) + Real(d8_tap(2)) * (m[2 * ld] - m[-2 * ld])
-             + Real(d8_tap(3)) * (m[3 * ld] - m[-3 * ld]) + Real(d8_tap(4)) * (m[4 * ld] - m[-4 * ld]);
-    }
-
-    // Stage 1 at one site: Laplacian and gradient of phi from its 3x3 box.
-    template <typename Real>
-    struct LocalTerms { Real lap, gy, gx; };
-
-    template <typename Real>
-    __device__ __forceinline__ LocalTerms<Real> local_terms(const Real* f, int ld, int i, int j, const Coefs<Real>& k)
-    {
-        const Real* u = f + (i - 1) * ld + j;
-        const Real* m = f + i * ld + j;
-        const Real* d = f + (i + 1) * ld + j;
-        // second differences along x per row, along y per column
-        Real sx_u = u[-1] - Real(2) * u[0] + u[1];
-        Real sx_m = m[-1] - Real(2) * m[0] + m[1];
-        Real sx_d = d[-1] - Real(2) * d[0] + d[1];
-        Real sy_l = u[-1] - Real(2) * m[-1] + d[-1];
-        Real sy_c = u[0] - Real(2) * m[0] + d[0];
-        Real sy_r = u[1] - Real(2) * m[1] + d[1];
-        Real second_x = Real(-0.25) * (sx_u + sx_d) + Real(1.5) * sx_m;
-        Real second_y = Real(-0.25) * (sy_l + sy_r) + Real(1.5) * sy_c;
-        LocalTerms<Real> t;
-        t.lap = k.ex * second_x + k.ey * second_y;
-        t.gx = k.dxInv * (Real(0.1) * ((u[1] - u[-1]) + (d[1] - d[-1])) + Real(0.3) * (m[1] - m[-1]));
-        t.gy = k.dyInv * (Real(0.1) * ((d[-1] - u[-1]) + (d[1] - u[1])) + Real(0.3) * (d[0] - u[0]));
-        return t;
-    }
-
-    // Compensated (Kahan) update phi += inc with residual `comp` carried between steps.
-    __device__ __forceinline__ float kahan_add(float phi, float inc, float& comp)
-    {
-        float y = inc - comp;
-        float t = phi + y;
-        comp = (t - phi) - y;
-        return t;
-    }
-
     template <typename Real, int TY, int TX, int COMP>
     __global__ void __launch_bounds__(256)
     step_tile_kernel(const Real* __restrict__ phi_in, Real* __restrict__ phi_out,
                      const __nv_bfloat16* comp_in, __nv_bfloat16* comp_out,  // may alias: each site reads/writes only its own
-                     StepParams p, int noise_mode, const Real* __restrict__ injected)
+                     StepParams p, const Canon<Real> k, int noise_mode, const Real* __restrict__ injected)
     {
         using G = TileGeom<TY, TX>;
         extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -137,7 +58,6 @@ namespace amb
         Real* J1Y = J2X + G::CY * G::CX;
         Real* J1X = J1Y + G::PY * TX;
 
-        const Coefs<Real> k(p);
         const int ny = p.ny, nx = p.nx;
         const int r0 = blockIdx.y * TY, c0 = blockIdx.x * TX;
         const int tid = threadIdx.x, nthr = blockDim.x;
@@ -152,7 +72,7 @@ namespace amb
         }
         __syncthreads();
 
-        // Stage 1: mu_p on the (TY+16) x (TX+16) box; mu_a on (TY+4)^2; J_c on (TY+2)^2.
+        // Stage A: mu_p on the (TY+16) x (TX+16) plus-shaped box; mu_a on (TY+4)^2; J_c on (TY+2)^2.
         for (int e = tid; e < G::MY * G::MX; e += nthr)
         {
             int bi = e / G::MX, bj = e - bi * G::MX;      // box coords, offset 8
@@ -160,27 +80,35 @@ namespace amb
             bool in_plus = (i >= 0 && i < TY) || (j >= 0 && j < TX);
             bool in_a = i >= -2 && i < TY + 2 && j >= -2 && j < TX + 2;
             if (!in_plus && !in_a) continue;
-            int pi = i + G::H, pj = j + G::H;
-            LocalTerms<Real> t = local_terms(PHI, G::LX, pi, pj, k);
-            Real f = PHI[pi * G::LX + pj];
-            MUP[e] = f * (k.a + f * (k.b + k.c * f)) - k.kappa * t.lap;
+            const Real* m = PHI + (i + G::H) * G::LX + (j + G::H);
+            const SiteA<Real> s = canon_stage_a(m - G::LX, m, m + G::LX, k);
+            MUP[e] = s.mup;
             if (in_a)
             {
-                MUA[(i + 2) * G::AX + (j + 2)] = k.lambda * (t.gy * t.gy + t.gx * t.gx);
+                MUA[(i + 2) * G::AX + (j + 2)] = s.mua;
                 if (i >= -1 && i < TY + 1 && j >= -1 && j < TX + 1)
                 {
-                    Real zl = k.zeta * t.lap;
-                    J2Y[(i + 1) * G::CX + (j + 1)] = zl * t.gy;
-                    J2X[(i + 1) * G::CX + (j + 1)] = zl * t.gx;
+                    J2Y[(i + 1) * G::CX + (j + 1)] = s.jcy;
+                    J2X[(i + 1) * G::CX + (j + 1)] = s.jcx;
                 }
             }
         }
         __syncthreads();
 
-        // Stage 2: J1 = J_p + J_r on the two arms, J2 = J_l + J_c on the box. With Philox
-        // noise and ncols % 4 == 0 the arms are walked by column quads, one Philox call per
+        // Stage B: J1 = -D8 mu_p + mag xi on the two arms, J2 = -Tj mu_a + J_c on the box. With
+        // Philox noise and ncols % 4 == 0 the arms are walked by column quads, one Philox call per
         // quad (the tile origin is a multiple of 4, so quads align with the noise's quads).
         const size_t plane = (size_t)ny * nx;
+        const auto j1y_at = [&](int i, int j, Real xi) {  // row i in [-4, TY+4), column j in [0, TX)
+            const Real* c = MUP + (i + 8) * G::MX + (j + 8);
+            constexpr int L = G::MX;
+            return rfma(k.mag, xi, canon_d8(k.ny8, c[-L], c[L], c[-2 * L], c[2 * L], c[-3 * L], c[3 * L], c[-4 * L],
+                                            c[4 * L]));
+        };
+        const auto j1x_at = [&](int i, int j, Real xi) {  // row i in [0, TY), column j in [-4, TX+4)
+            const Real* c = MUP + (i + 8) * G::MX + (j + 8);
+            return rfma(k.mag, xi, canon_d8(k.nx8, c[-1], c[1], c[-2], c[2], c[-3], c[3], c[-4], c[4]));
+        };
         if (noise_mode == NOISE_PHILOX && nx % 4 == 0)
         {
             constexpr int QY = TX / 4, QQ = G::QX / 4;
@@ -190,8 +118,7 @@ namespace amb
                 float z[4];
                 noise_quad(p.seed, p.step, wrap_index(r0 + i, ny), wrap_index(c0 + j, nx), 0, z);
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    J1Y[(i + 4) * TX + j + q] = -(k.dyInv * d8_y(MUP, G::MX, i + 8, j + q + 8)) + k.mag * Real(z[q]);
+                for (int q = 0; q < 4; ++q) J1Y[(i + 4) * TX + j + q] = j1y_at(i, j + q, Real(z[q]));
             }
             for (int e = tid; e < TY * QQ; e += nthr)
             {
@@ -199,8 +126,7 @@ namespace amb
                 float z[4];
                 noise_quad(p.seed, p.step, wrap_index(r0 + i, ny), wrap_index(c0 + j, nx), 1, z);
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    J1X[i * G::QX + j + q + 4] = -(k.dxInv * d8_x(MUP, G::MX, i + 8, j + q + 8)) + k.mag * Real(z[q]);
+                for (int q = 0; q < 4; ++q) J1X[i * G::QX + j + q + 4] = j1x_at(i, j + q, Real(z[q]));
             }
         }
         else
@@ -215,7 +141,7 @@ namespace amb
                     xi = noise_mode == NOISE_PHILOX ? Real(noise_normal(p.seed, p.step, gr, gc, 0))
                                                     : injected[(size_t)gr * nx + gc];
                 }
-                J1Y[e] = -(k.dyInv * d8_y(MUP, G::MX, i + 8, j + 8)) + k.mag * xi;
+                J1Y[e] = j1y_at(i, j, xi);
             }
             for (int e = tid; e < TY * G::QX; e += nthr)
             {
@@ -227,37 +153,51 @@ namespace amb
                     xi = noise_mode == NOISE_PHILOX ? Real(noise_normal(p.seed, p.step, gr, gc, 1))
                                                     : injected[plane + (size_t)gr * nx + gc];
                 }
-                J1X[e] = -(k.dxInv * d8_x(MUP, G::MX, i + 8, j + 8)) + k.mag * xi;
+                J1X[e] = j1x_at(i, j, xi);
             }
         }
         for (int e = tid; e < G::CY * G::CX; e += nthr)
         {
-            int ci = e / G::CX, cj = e - ci * G::CX;      // offset 1
-            J2Y[e] += -(k.dyInv * tj_y(MUA, G::AX, ci + 1, cj + 1));
-            J2X[e] += -(k.dxInv * tj_x(MUA, G::AX, ci + 1, cj + 1));
+            int ci = e / G::CX, cj = e - ci * G::CX;      // box offset 1: rows ci-1..ci+1 of mu_a are its rows ci..ci+2
+            const Real* a0 = MUA + ci * G::AX + cj + 1;     // mu_a row above, centre column
+            const Real* a1 = a0 + G::AX;
+            const Real* a2 = a1 + G::AX;
+            const Real sx_m = canon_smooth(a0[-1], a0[0], a0[1], k), sx_p = canon_smooth(a2[-1], a2[0], a2[1], k);
+            const Real dx_m = rsub(a0[1], a0[-1]), dx_0 = rsub(a1[1], a1[-1]), dx_p = rsub(a2[1], a2[-1]);
+            J2Y[e] = canon_j2y(sx_m, sx_p, J2Y[e], k);
+            J2X[e] = canon_j2x(dx_m, dx_0, dx_p, J2X[e], k);
         }
         __syncthreads();
 
-        // Stage 3: div J and the update.
+        // Stage C: div J and the update.
         for (int e = tid; e < TY * TX; e += nthr)
         {
             int i = e / TX, j = e - i * TX;
             int gr = r0 + i, gc = c0 + j;
             if (gr >= ny || gc >= nx) continue;
-            Real div = k.dyInv * tj_y(J2Y, G::CX, i + 1, j + 1) + k.dxInv * tj_x(J2X, G::CX, i + 1, j + 1)
-                     + k.dyInv * d8_y(J1Y, TX, i + 4, j) + k.dxInv * d8_x(J1X, G::QX, i, j + 4);
-            Real f = PHI[(i + G::H) * G::LX + (j + G::H)];
-            size_t gi = (size_t)gr * nx + gc;
+            const Real* y0 = J2Y + i * G::CX + j + 1;       // J2 rows i-1, i, i+1 at J2 rows i, i+1, i+2
+            const Real* y2 = y0 + 2 * G::CX;
+            const Real* x0 = J2X + i * G::CX + j + 1;
+            const Real* x1 = x0 + G::CX;
+            const Real* x2 = x1 + G::CX;
+            const Real divtj = canon_divtj(canon_smooth(y0[-1], y0[0], y0[1], k), canon_smooth(y2[-1], y2[0], y2[1], k),
+                                           rsub(x0[1], x0[-1]), rsub(x1[1], x1[-1]), rsub(x2[1], x2[-1]), k);
+            const Real* cy = J1Y + (i + 4) * TX + j;
+            const Real dy8 = canon_d8(k.py8, cy[-TX], cy[TX], cy[-2 * TX], cy[2 * TX], cy[-3 * TX], cy[3 * TX],
+                                      cy[-4 * TX], cy[4 * TX]);
+            const Real* cx = J1X + i * G::QX + j + 4;
+            const Real dx8 = canon_d8(k.px8, cx[-1], cx[1], cx[-2], cx[2], cx[-3], cx[3], cx[-4], cx[4]);
+            const Real f = PHI[(i + G::H) * G::LX + (j + G::H)];
+            const size_t gi = (size_t)gr * nx + gc;
             if constexpr (COMP == COMP_BF16)
             {
-                float comp = __bfloat162float(comp_in[gi]);
-                float nf = kahan_add(float(f), -float(k.dt) * float(div), comp);
-                phi_out[gi] = Real(nf);
-                comp_out[gi] = __float2bfloat16_rn(comp);
+                float r = __bfloat162float(comp_in[gi]);
+                phi_out[gi] = canon_update_comp(f, dx8, divtj, dy8, r, k);
+                comp_out[gi] = __float2bfloat16_rn(r);
             }
             else
             {
-                phi_out[gi] = f - k.dt * div;
+                phi_out[gi] = canon_update(f, dx8, divtj, dy8, k);
             }
         }
     }

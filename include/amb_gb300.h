@@ -160,8 +160,8 @@ int amb_step_f32(const amb_stencil* stencil, const amb_model* model, uint64_t se
  * fastest configuration and its time per step. The result is cached per (device, shape,
  * compensated, noise); later calls return the cached entry, and AMB_KERNEL_AUTO in
  * amb_step_f32 / amb_step_f32_ex uses it. Synchronous; allocates 2-3 fields of scratch. The
- * two FP32 kernels agree to FP32 rounding, not bitwise: request a kernel explicitly for
- * results that must not depend on a timing. */
+ * FP32 kernels evaluate the same operations in the same order at every site, so their results
+ * are bitwise equal: what the autotuner picks changes the time, never the field. */
 int amb_autotune_f32(const amb_stencil* stencil, const amb_model* model, int nrows, int ncols, int compensated,
                      int probe_steps, void* stream, amb_kernel_config* best, double* us_per_step);
 

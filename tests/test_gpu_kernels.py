@@ -3,10 +3,10 @@ device-pointer C ABI (amb_step_f32_ex).
 
 Covers the warp-pair sliding kernel's decomposition (row segments, strips, the
 overlapping last strip, periodic wrap of the row window), its Philox and
-injected noise, and both FP32 storage modes. Tolerances are stated per test:
-the two FP32 kernels evaluate the same operators in a different rounding
-order, so they agree to FP32 rounding, not bitwise; one kernel under different
-decompositions agrees bitwise.
+injected noise, and both FP32 storage modes. Both FP32 kernels (tile, sliding)
+evaluate the same operations in the same order at every site (amb_canon.cuh),
+so they agree bitwise with each other and under any decomposition; against the
+FP64 oracle the tolerances are stated per test.
 """
 import ctypes
 
@@ -57,15 +57,15 @@ def initial(shape, seed=0):
 @pytest.mark.parametrize("shape", [(256, 256), (200, 140), (37, 340), (17, 256), (96, 448), (5, 136), (128, 128), (40, 112), (64, 116)])
 @pytest.mark.parametrize("T", [0.0, 0.05])
 def test_sliding_matches_tile(shape, T):
-    """Both FP32 kernels, 30 steps, plain FP32 and compensated: max |diff| < 2e-6
-    (different rounding order of the same operators; fields ~0.4)."""
+    """The tile and sliding FP32 kernels, 30 steps, plain FP32 and compensated: bitwise equal
+    (the same arithmetic at every site, only the work decomposition differs)."""
     field = initial(shape, seed=shape[0])
     p = Params(T=T, **AMB)
     for comp in (False, True):
         tile = run_f32(field, p, 30, kernel=1, comp=comp)
         slid = run_f32(field, p, 30, kernel=2, comp=comp)
         assert np.isfinite(slid).all()
-        assert np.abs(tile - slid).max() < 2e-6, (comp, np.abs(tile - slid).max())
+        assert np.array_equal(tile, slid), (comp, np.abs(tile - slid).max())
 
 
 @pytest.mark.parametrize("seg_rows,pairs", [(0, 0), (16, 1), (37, 2), (100, 4), (1000, 2), (1, 1)])
@@ -166,3 +166,21 @@ def test_integrator_explicit_launch_shape():
     sim.run(10)
     ref = run_f32(field, p, 10, kernel=2, seg_rows=16, pairs=4, comp=False, seed=7)
     assert np.array_equal(sim.field, ref)
+
+
+def test_kernels_match_pinned_bits():
+    """Every FP32 kernel reproduces the pinned SHA-256 of the sliding kernel's output (and, for
+    f32c, its residual plane), recorded on a GB300 by tests/golden/make_f32_pins.py: no kernel
+    change may alter a bit of the step's results unnoticed."""
+    import json
+    import os
+    from conftest import GOLDEN
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_f32_pins as M
+    with open(os.path.join(GOLDEN, "f32_kernel_pins.json")) as f:
+        pins = json.load(f)["pins"]
+    for _, shape, comp, T in M.all_cases():
+        want = pins[M.case_name("sliding", shape, comp, T)]
+        for kernel in (1, 2):
+            assert M.run_case(kernel, shape, comp, T) == want, (kernel, shape, comp, T)
