@@ -176,14 +176,16 @@ class Integrator:
         seed: 64-bit key of the Philox noise; ``None`` draws one from the OS,
             like the reference's non-deterministic seed.
         device: CUDA device (default: current).
-        kernel: "auto", "tile" or "sliding" (FP32 kernel choice).
+        kernel: "auto", "tile" or "sliding" (FP32 kernel choice; FP64 always runs the tile kernel).
         autotune: with kernel="auto" and FP32 storage, time the candidate kernels and
             launch shapes for this grid once per process (``amb_autotune_f32``) and use
             the fastest; otherwise a shape heuristic decides. The FP32 kernels give
             bitwise equal fields (the same arithmetic at every site), so the choice
             changes the time, never the result.
-        launch: explicit launch shape of the sliding kernel, {"seg_rows": h, "pairs_per_cta": p}
-            (FP32 storage with kernel="sliding"; e.g. a configuration the autotuner reported).
+        launch: explicit launch shape: for kernel="sliding" (FP32 storage) {"seg_rows": h,
+            "pairs_per_cta": p}; for kernel="tile" {"pairs_per_cta": g (256-thread groups per CTA),
+            "persistent": bool (all steps of a run() in one launch)}; e.g. a configuration the
+            autotuner reported.
     """
 
     def __init__(self, field, stencil, model, *, precision: str = "f64", seed: int | None = None,
@@ -225,10 +227,11 @@ class Integrator:
         self.set_field(host)
         self._launch_cfg = None
         if launch is not None:
-            if precision == "f64" or kernel != "sliding":
-                raise ValueError('launch= applies to FP32 storage with kernel="sliding"')
+            if kernel not in ("sliding", "tile") or (precision == "f64" and kernel != "tile"):
+                raise ValueError('launch= applies to kernel="sliding" (FP32 storage) or kernel="tile"')
+            flags = N.AMB_FLAG_PERSISTENT if launch.get("persistent", False) else 0
             self._launch_cfg = N.amb_kernel_config(_KERNELS[kernel], int(launch.get("seg_rows", 0)),
-                                                   int(launch.get("pairs_per_cta", 0)), 0)
+                                                   int(launch.get("pairs_per_cta", 0)), flags)
         self._tuned = None
         if autotune and kernel == "auto" and precision != "f64":
             cfg, us = N.amb_kernel_config(), ctypes.c_double()
@@ -237,7 +240,8 @@ class Integrator:
                                         ctypes.byref(us)))
             names = {N.AMB_KERNEL_TILE: "tile", N.AMB_KERNEL_SLIDING: "sliding"}
             self._tuned = {"kernel": names.get(cfg.kernel, "auto"), "seg_rows": cfg.seg_rows,
-                           "pairs_per_cta": cfg.pairs_per_cta, "us_per_step": us.value}
+                           "pairs_per_cta": cfg.pairs_per_cta,
+                           "persistent": bool(cfg.flags & N.AMB_FLAG_PERSISTENT), "us_per_step": us.value}
         del lib
 
     # -------------------------------------------------------------- plumbing
@@ -308,9 +312,10 @@ class Integrator:
             if self._events is not None:
                 self._events[0].record()
             if self._precision == "f64":
-                rc = lib.amb_step_f64(ctypes.byref(self._s), ctypes.byref(self._m), self._seed, self._ny, self._nx,
-                                      cur.data_ptr(), other.data_ptr(), self._timestep, nsteps, None, stream,
-                                      ctypes.byref(in_spare))
+                rc = lib.amb_step_f64_ex(ctypes.byref(self._s), ctypes.byref(self._m), self._seed, self._ny,
+                                         self._nx, cur.data_ptr(), other.data_ptr(), self._timestep, nsteps, None,
+                                         ctypes.byref(self._launch_cfg) if self._launch_cfg is not None else None,
+                                         stream, ctypes.byref(in_spare))
             else:
                 res = self._residual.data_ptr() if self._residual is not None else None
                 if self._launch_cfg is not None:

@@ -37,7 +37,10 @@ class amb_model(ctypes.Structure):
 
 class amb_kernel_config(ctypes.Structure):
     _fields_ = [("kernel", ctypes.c_int), ("seg_rows", ctypes.c_int), ("pairs_per_cta", ctypes.c_int),
-                ("reserved", ctypes.c_int)]
+                ("flags", ctypes.c_int)]
+
+
+AMB_FLAG_PERSISTENT = 1
 
 
 _VP = ctypes.c_void_p
@@ -66,6 +69,8 @@ SIGNATURES = {
     "amb_integrator_get_model": (_I, [_VP, _MP]),
     "amb_integrator_get_shape": (_I, [_VP, _IP, _IP, _IP]),
     "amb_step_f64": (_I, [_SP, _MP, _U64, _I, _I, _VP, _VP, _I64, _I, _VP, _VP, _IP]),
+    "amb_step_f64_ex": (_I, [_SP, _MP, _U64, _I, _I, _VP, _VP, _I64, _I, _VP, ctypes.POINTER(amb_kernel_config),
+                             _VP, _IP]),
     "amb_step_f32": (_I, [_SP, _MP, _U64, _I, _I, _VP, _VP, _VP, _I64, _I, _VP, _I, _VP, _IP]),
     "amb_step_f32_ex": (_I, [_SP, _MP, _U64, _I, _I, _VP, _VP, _VP, _I64, _I, _VP, ctypes.POINTER(amb_kernel_config),
                              _VP, _IP]),

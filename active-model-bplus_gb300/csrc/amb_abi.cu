@@ -84,28 +84,79 @@ extern "C" const char* amb_last_error(void) { return g_last_error.c_str(); }
 
 // ------------------------------------------------------------------ steps
 
-extern "C" int amb_step_f64(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows, int ncols,
-                            double* field, double* spare, int64_t step0, int nsteps, const double* injected_noise,
-                            void* stream, int* result_in_spare)
+namespace
+{
+    bool capturing(cudaStream_t s)
+    {
+        cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+        return cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone;
+    }
+
+    // Steps of the tile kernel: one launch per step, or all of them in one persistent launch.
+    template <typename Real>
+    int tile_steps(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows, int ncols,
+                   Real* field, Real* spare, __nv_bfloat16* res, int comp, int64_t step0, int nsteps,
+                   const Real* injected_noise, const amb_kernel_config& cfg, cudaStream_t stream,
+                   int* result_in_spare, const char* name)
+    {
+        const size_t n = size_t(nrows) * ncols;
+        const int mode = noise_mode_for(model, injected_noise);
+        const int groups = cfg.pairs_per_cta == 0 ? 1 : cfg.pairs_per_cta;
+        if ((cfg.flags & AMB_FLAG_PERSISTENT) && nsteps > 1 && !capturing(stream))
+        {
+            amb::StepParams p = make_params(stencil, model, seed, nrows, ncols, step0);
+            cudaError_t e = amb::launch_steps_tile_persistent<Real>(field, spare, res, comp, p, mode, injected_noise,
+                                                                    nsteps, groups, stream);
+            if (e != cudaSuccess) return cuda_fail(e, name);
+            if (result_in_spare) *result_in_spare = nsteps & 1;
+            return AMB_OK;
+        }
+        Real* cur = field;
+        Real* nxt = spare;
+        for (int s = 0; s < nsteps; ++s)
+        {
+            amb::StepParams p = make_params(stencil, model, seed, nrows, ncols, step0 + s);
+            const Real* inj = injected_noise ? injected_noise + size_t(s) * 2 * n : nullptr;
+            cudaError_t e = amb::launch_step_tile<Real>(cur, nxt, res, comp, p, mode, inj, groups, stream);
+            if (e != cudaSuccess) return cuda_fail(e, name);
+            std::swap(cur, nxt);
+        }
+        if (result_in_spare) *result_in_spare = (cur == spare) ? 1 : 0;
+        return AMB_OK;
+    }
+
+    int check_config(const amb_kernel_config& cfg, int max_kernel)
+    {
+        if (cfg.kernel < AMB_KERNEL_AUTO || cfg.kernel > max_kernel) return fail(AMB_ERR_INVALID, "unknown kernel selector");
+        if (cfg.seg_rows < 0 || cfg.pairs_per_cta < 0 || cfg.pairs_per_cta > 4 || cfg.pairs_per_cta == 3)
+            return fail(AMB_ERR_INVALID, "kernel config: seg_rows >= 0, pairs_per_cta in {0, 1, 2, 4}");
+        if (cfg.flags & ~AMB_FLAG_PERSISTENT) return fail(AMB_ERR_INVALID, "kernel config: unknown flags");
+        return AMB_OK;
+    }
+}
+
+extern "C" int amb_step_f64_ex(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows,
+                               int ncols, double* field, double* spare, int64_t step0, int nsteps,
+                               const double* injected_noise, const amb_kernel_config* config, void* stream,
+                               int* result_in_spare)
 {
     if (int rc = check_shape(nrows, ncols)) return rc;
     if (int rc = check_params(stencil, model)) return rc;
     if (!field || !spare || field == spare) return fail(AMB_ERR_INVALID, "field and spare must be distinct device buffers");
     if (nsteps < 0) return fail(AMB_ERR_INVALID, "nsteps must be >= 0");
-    const size_t n = size_t(nrows) * ncols;
-    const int mode = noise_mode_for(model, injected_noise);
-    double* cur = field;
-    double* nxt = spare;
-    for (int s = 0; s < nsteps; ++s)
-    {
-        amb::StepParams p = make_params(stencil, model, seed, nrows, ncols, step0 + s);
-        const double* inj = injected_noise ? injected_noise + size_t(s) * 2 * n : nullptr;
-        cudaError_t e = amb::launch_step_tile<double>(cur, nxt, nullptr, amb::COMP_NONE, p, mode, inj, as_stream(stream));
-        if (e != cudaSuccess) return cuda_fail(e, "amb_step_f64");
-        std::swap(cur, nxt);
-    }
-    if (result_in_spare) *result_in_spare = (cur == spare) ? 1 : 0;
-    return AMB_OK;
+    amb_kernel_config cfg{AMB_KERNEL_AUTO, 0, 0, 0};
+    if (config) cfg = *config;
+    if (int rc = check_config(cfg, AMB_KERNEL_TILE)) return rc;
+    return tile_steps<double>(stencil, model, seed, nrows, ncols, field, spare, nullptr, amb::COMP_NONE, step0, nsteps,
+                              injected_noise, cfg, as_stream(stream), result_in_spare, "amb_step_f64");
+}
+
+extern "C" int amb_step_f64(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows, int ncols,
+                            double* field, double* spare, int64_t step0, int nsteps, const double* injected_noise,
+                            void* stream, int* result_in_spare)
+{
+    return amb_step_f64_ex(stencil, model, seed, nrows, ncols, field, spare, step0, nsteps, injected_noise, nullptr,
+                           stream, result_in_spare);
 }
 
 namespace
@@ -130,9 +181,7 @@ extern "C" int amb_step_f32_ex(const amb_stencil* stencil, const amb_model* mode
         if (amb::autotune_lookup(nrows, ncols, residual != nullptr, model->temperature > 0 && !injected_noise, &tuned))
             cfg = tuned;  // a sliding choice still falls back to the tile kernel on unaligned buffers below
     }
-    if (cfg.kernel < AMB_KERNEL_AUTO || cfg.kernel > AMB_KERNEL_SLIDING) return fail(AMB_ERR_INVALID, "unknown kernel selector");
-    if (cfg.seg_rows < 0 || cfg.pairs_per_cta < 0 || cfg.pairs_per_cta > 4 || cfg.pairs_per_cta == 3)
-        return fail(AMB_ERR_INVALID, "kernel config: seg_rows >= 0, pairs_per_cta in {0, 1, 2, 4}");
+    if (int rc = check_config(cfg, AMB_KERNEL_SLIDING)) return rc;
     const size_t n = size_t(nrows) * ncols;
     const int mode = noise_mode_for(model, injected_noise);
     const int comp = residual ? amb::COMP_BF16 : amb::COMP_NONE;
@@ -151,6 +200,9 @@ extern "C" int amb_step_f32_ex(const amb_stencil* stencil, const amb_model* mode
     }
     else if (cfg.kernel == AMB_KERNEL_AUTO)
         sliding = fits;
+    if (!sliding)
+        return tile_steps<float>(stencil, model, seed, nrows, ncols, field, spare, res, comp, step0, nsteps,
+                                 injected_noise, cfg, as_stream(stream), result_in_spare, "amb_step_f32");
     const int pairs_code = cfg.pairs_per_cta == 1 ? 1 : cfg.pairs_per_cta == 4 ? 3 : cfg.pairs_per_cta == 2 ? 2 : 0;
     const int variant = (cfg.seg_rows << 4) | pairs_code;
     float* cur = field;
@@ -159,8 +211,7 @@ extern "C" int amb_step_f32_ex(const amb_stencil* stencil, const amb_model* mode
     {
         amb::StepParams p = make_params(stencil, model, seed, nrows, ncols, step0 + s);
         const float* inj = injected_noise ? injected_noise + size_t(s) * 2 * n : nullptr;
-        cudaError_t e = sliding ? amb::launch_step_f32_sliding(cur, nxt, res, comp, p, mode, inj, variant, as_stream(stream))
-                                : amb::launch_step_tile<float>(cur, nxt, res, comp, p, mode, inj, as_stream(stream));
+        cudaError_t e = amb::launch_step_f32_sliding(cur, nxt, res, comp, p, mode, inj, variant, as_stream(stream));
         if (e != cudaSuccess) return cuda_fail(e, "amb_step_f32");
         std::swap(cur, nxt);
     }

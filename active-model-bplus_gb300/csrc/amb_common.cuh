@@ -108,26 +108,59 @@ namespace amb
     // Box-Muller on one pair of 32-bit words with 24-bit uniforms:
     // ua = ((xa >> 8) + 1) 2^-24 in (0,1], ub = (xb >> 8) 2^-24 in [0,1);
     // r = sqrt(-2 ln ua), theta = 2 pi (ub - 1/2); returns (r cos theta, r sin theta).
-    // Evaluated in single precision. -ln(ua) uses the fast
+    // Evaluated in single precision, every operation rounded once as written (no contraction),
+    // so the scalar and the packed form below give the same bits. -ln(ua) uses the fast
     // hardware logarithm (__logf) where ua <= 31/32; closer to 1 its absolute
     // error would rival ln(ua) itself, so there -ln(1 - v), v = 1 - ua (exact),
     // is summed from the Mercator series v + v^2/2 + ... + v^5/5 (truncation
-    // below 1e-8 relative for v < 1/32). |theta| <= pi keeps __sincosf in its
-    // accurate range.
+    // below 1e-8 relative for v < 1/32), as 2v (1 + v (1/2 + v (1/3 + v (1/4 + v/5)))).
+    // |theta| <= pi keeps __sincosf in its accurate range.
     __device__ __forceinline__ float2 box_muller_f32(uint32_t xa, uint32_t xb)
     {
-        uint32_t ka = xa >> 8;
-        float ua = float(ka + 1u) * (1.0f / 16777216.0f);
-        float v = float(16777215u - ka) * (1.0f / 16777216.0f);
-        float ub = float(xb >> 8) * (1.0f / 16777216.0f);
+        const uint32_t ka = xa >> 8;
+        const float ua = __fmul_rn(float(ka + 1u), 1.0f / 16777216.0f);
+        const float v = __fmul_rn(float(16777215u - ka), 1.0f / 16777216.0f);
+        const float ub = __fmul_rn(float(xb >> 8), 1.0f / 16777216.0f);
         // both branches evaluated and selected: a divergent branch would make most warps run both anyway
-        float t_series = 2.0f * v * (1.0f + v * (0.5f + v * (0.333333343f + v * (0.25f + v * 0.2f))));
-        float t_log = -2.0f * __logf(ua);
-        float t = v < 0.03125f ? t_series : t_log;
-        float r = t * rsqrtf(fmaxf(t, 1e-30f));
-        float s, c;
-        __sincosf(6.283185307179586f * (ub - 0.5f), &s, &c);
-        return make_float2(r * c, r * s);
+        float ser = __fmaf_rn(v, 0.2f, 0.25f);
+        ser = __fmaf_rn(v, ser, 0.333333343f);
+        ser = __fmaf_rn(v, ser, 0.5f);
+        ser = __fmaf_rn(v, ser, 1.0f);
+        const float t_series = __fmul_rn(__fmul_rn(2.0f, v), ser);
+        const float t_log = __fmul_rn(-2.0f, __logf(ua));
+        const float t = v < 0.03125f ? t_series : t_log;
+        const float r = __fmul_rn(t, rsqrtf(fmaxf(t, 1e-30f)));
+        float sn, cs;
+        __sincosf(__fmul_rn(6.283185307179586f, __fadd_rn(ub, -0.5f)), &sn, &cs);
+        return make_float2(__fmul_rn(r, cs), __fmul_rn(r, sn));
+    }
+
+    // box_muller_f32 on two independent pairs of words, (xa.x, xb.x) and (xa.y, xb.y): the
+    // integer steps and the hardware approximations per pair, the floating-point steps as packed
+    // FP32 pairs (each half rounded as the scalar operation). zc = (r cos) and zs = (r sin) of the
+    // two pairs: box_muller_f32(xa.x, xb.x) == (zc.x, zs.x), box_muller_f32(xa.y, xb.y) == (zc.y, zs.y).
+    __device__ __forceinline__ void box_muller_f32x2(uint2 xa, uint2 xb, float2& zc, float2& zs)
+    {
+        const auto d = [](float c) { return make_float2(c, c); };
+        const uint32_t kx = xa.x >> 8, ky = xa.y >> 8;
+        const float2 inv24 = d(1.0f / 16777216.0f);
+        const float2 ua = __fmul2_rn(make_float2(float(kx + 1u), float(ky + 1u)), inv24);
+        const float2 v = __fmul2_rn(make_float2(float(16777215u - kx), float(16777215u - ky)), inv24);
+        const float2 ub = __fmul2_rn(make_float2(float(xb.x >> 8), float(xb.y >> 8)), inv24);
+        float2 ser = __ffma2_rn(v, d(0.2f), d(0.25f));
+        ser = __ffma2_rn(v, ser, d(0.333333343f));
+        ser = __ffma2_rn(v, ser, d(0.5f));
+        ser = __ffma2_rn(v, ser, d(1.0f));
+        const float2 t_series = __fmul2_rn(__fmul2_rn(d(2.0f), v), ser);
+        const float2 t_log = __fmul2_rn(d(-2.0f), make_float2(__logf(ua.x), __logf(ua.y)));
+        const float2 t = make_float2(v.x < 0.03125f ? t_series.x : t_log.x, v.y < 0.03125f ? t_series.y : t_log.y);
+        const float2 r = __fmul2_rn(t, make_float2(rsqrtf(fmaxf(t.x, 1e-30f)), rsqrtf(fmaxf(t.y, 1e-30f))));
+        const float2 th = __fmul2_rn(d(6.283185307179586f), __fadd2_rn(ub, d(-0.5f)));
+        float sx, cx, sy, cy;
+        __sincosf(th.x, &sx, &cx);
+        __sincosf(th.y, &sy, &cy);
+        zc = __fmul2_rn(r, make_float2(cx, cy));
+        zs = __fmul2_rn(r, make_float2(sx, sy));
     }
 
     // One standard normal of the (seed, step) noise field at (row, col, comp). Both field

@@ -34,6 +34,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 
 namespace amb
 {
@@ -229,8 +230,9 @@ namespace amb
                 U4 ctr{uint32_t(gcol) >> 2, uint32_t(grow), uint32_t(uint64_t(p.step)),
                        (uint32_t(uint64_t(p.step) >> 32) << 1) | uint32_t(comp)};
                 U4 q = philox4x32_10_rk(ctr, k.rk0, k.rk1);
-                float2 p0 = box_muller_f32(q.x, q.y), p1 = box_muller_f32(q.z, q.w);
-                z[0] = p0.x; z[1] = p0.y; z[2] = p1.x; z[3] = p1.y;
+                float2 zc, zs;  // (r cos, r sin) of the draws (x, y) and (z, w)
+                box_muller_f32x2(make_uint2(q.x, q.z), make_uint2(q.y, q.w), zc, zs);
+                z[0] = zc.x; z[1] = zs.x; z[2] = zc.y; z[3] = zs.y;
             }
             else if constexpr (NOISE == NOISE_INJECTED)
             {
@@ -262,7 +264,18 @@ namespace amb
             return t;
         }
 
+        // Pointer to row slot i (0 <= i < 8) of a window of 8 consecutive ring rows that starts at
+        // slot b of a ring of N slots: slots b..N-1 from `at_b`, the wrapped ones from `at_b` - N rows.
+        // One compare and one select per row; the row offset is a constant of the load.
+        template <int N>
+        __device__ __forceinline__ const float* ring_row(const float* at_b, int b, int i)
+        {
+            return (b < N - i ? at_b : at_b - N * kCols) + i * kCols;
+        }
+
         // Producer warp: stage A, the mu_p ring, J1_y and its noise; streams phi rows in by TMA.
+        // Rounds 1..8 feed no J1_y row that an output reads and rounds 1..16 no DY8 row: they run
+        // the body without those parts (the rounds' other results are the same).
         template <int NOISE>
         __device__ __forceinline__ void producer(PairSmem& sm, const float* __restrict__ phi_in, const StepParams& p,
                                                  const Coef& k, const float* __restrict__ injected, const Task& t,
@@ -296,14 +309,13 @@ namespace amb
                 fm[q] = sm.phi[0][own - 1 + q];
                 fz[q] = sm.phi[1][own - 1 + q];
             }
-            // Rounds are not unrolled (code size): the row rings live in shared memory.
-            float xin[4];    // xi_y of this round's J1_y row, formed one round ahead
-            normals<NOISE>(p, k, injected, wrap_index(t.r0 - 12, ny), gcol, 0, xin);
+            float xin[4] = {0.f, 0.f, 0.f, 0.f};  // xi_y of this round's J1_y row, formed one round ahead
+            int nrow = 0;    // global row of the next round's J1_y noise
             int ms = 1;      // mu_p ring slot of row kl  (kl mod 10)
-            int js = 6;      // J1_y ring slot of row kl-4 ((kl - 4) mod 9)
-#pragma unroll 1
-            for (int kl = 1; kl <= total; ++kl)
-            {
+            int js = 5;      // J1_y ring slot of row kl-4 ((kl - 4) mod 9), from round 9 on
+
+            const auto round = [&](int kl, auto j1_tag, auto dy_tag) {
+                constexpr bool J1 = decltype(j1_tag)::value, DY = decltype(dy_tag)::value;
                 const int mnew = kl + 1;
                 if (!failed)
                 {
@@ -369,41 +381,36 @@ namespace amb
                 sts4(&h[0][4 * lane], mua);
                 sts4(&h[1][4 * lane], jcy);
                 sts4(&h[2][4 * lane], jcx);
-                // ---- J1_y at local row kl-4 from mu_p rows kl-8..kl (this lane's own columns).
-                // Outputs start at local row 9 and read J1_y rows >= 5 (rounds >= 9); earlier rounds
-                // compute values nobody reads, which keeps the round one straight-line block.
+                if constexpr (J1)
                 {
+                    // ---- J1_y at local row kl-4 from mu_p rows kl-8..kl (this lane's own columns)
+                    const int bm = ms + 2 < kMupRing ? ms + 2 : ms + 2 - kMupRing;  // slot of row kl-8
+                    const float* mb = &sm.mup[bm][4 * lane];
                     float4 m[9];
 #pragma unroll
                     for (int i = 0; i < 8; ++i)
-                    {
-                        if (i == 4) continue;
-                        int slot = ms - 8 + i;
-                        slot += slot < 0 ? kMupRing : 0;
-                        m[i] = lds4(&sm.mup[slot][4 * lane]);
-                    }
+                        if (i != 4) m[i] = lds4(ring_row<kMupRing>(mb, bm, i));
                     m[4] = make_float4(0.f, 0.f, 0.f, 0.f);  // the centre tap has weight 0
                     m[8] = make_float4(mup[0], mup[1], mup[2], mup[3]);
                     const float2 xlo = make_float2(xin[0], xin[1]), xhi = make_float2(xin[2], xin[3]);
                     // noise of the next round's J1_y row, formed now so its Philox chain overlaps this round
-                    normals<NOISE>(p, k, injected, wrap_index(t.r0 - 12 + kl, ny), gcol, 0, xin);
+                    normals<NOISE>(p, k, injected, nrow, gcol, 0, xin);
+                    nrow = nrow + 1 == ny ? 0 : nrow + 1;
                     float2 slo, shi;
                     d8y_pairs(m, k.ny8p, slo, shi);
                     slo = __ffma2_rn(k.magp, xlo, slo);
                     shi = __ffma2_rn(k.magp, xhi, shi);
                     const float j1y[4] = {slo.x, slo.y, shi.x, shi.y};
                     sts4(&sm.j1y[js][4 * lane], j1y);
-                    // ---- DY8 at local row kl-8 from J1_y rows kl-12..kl-4 (read by outputs from round 17)
+                    if constexpr (DY)
                     {
+                        // ---- DY8 at local row kl-8 from J1_y rows kl-12..kl-4
+                        const int bj = js + 1 < kJ1Ring ? js + 1 : js + 1 - kJ1Ring;  // slot of row kl-12
+                        const float* jb = &sm.j1y[bj][4 * lane];
                         float4 j[9];
 #pragma unroll
                         for (int i = 0; i < 8; ++i)
-                        {
-                            if (i == 4) continue;
-                            int slot = js - 8 + i;
-                            slot += slot < 0 ? kJ1Ring : 0;
-                            j[i] = lds4(&sm.j1y[slot][4 * lane]);
-                        }
+                            if (i != 4) j[i] = lds4(ring_row<kJ1Ring>(jb, bj, i));
                         j[4] = make_float4(0.f, 0.f, 0.f, 0.f);
                         j[8] = make_float4(j1y[0], j1y[1], j1y[2], j1y[3]);
                         float2 dlo, dhi;
@@ -411,9 +418,9 @@ namespace amb
                         const float dy8[4] = {dlo.x, dlo.y, dhi.x, dhi.y};
                         sts4(&h[3][4 * lane], dy8);
                     }
+                    js = js + 1 == kJ1Ring ? 0 : js + 1;
                 }
                 ms = ms + 1 == kMupRing ? 0 : ms + 1;
-                js = js + 1 == kJ1Ring ? 0 : js + 1;
                 // ---- refill: local row kl-10 has been read by everyone (barrier kl-1); fetch row kl+6
                 if (lane == 0 && !failed && kl + 6 < nrows)
                 {
@@ -422,12 +429,25 @@ namespace amb
                 }
                 if (!failed && kl + 6 < nrows) issued = kl + 6;
                 pair_sync(bar_id);
-            }
+            };
+            using F = std::false_type;
+            using T = std::true_type;
+#pragma unroll 1
+            for (int kl = 1; kl <= 8; ++kl) round(kl, F{}, F{});
+            // J1_y rows from local row 5 (round 9) on: xi_y of that row (global r0 - 4) now
+            nrow = wrap_index(t.r0 - 4, ny);
+            normals<NOISE>(p, k, injected, nrow, gcol, 0, xin);
+            nrow = nrow + 1 == ny ? 0 : nrow + 1;
+#pragma unroll 1
+            for (int kl = 9; kl <= 16; ++kl) round(kl, T{}, F{});
+#pragma unroll 1
+            for (int kl = 17; kl <= total; ++kl) round(kl, T{}, T{});
             if (failed)  // drain this pair's copies in flight (bounded) before the CTA can exit
                 for (int m = waited + 1; m <= issued; ++m) mbar_wait(&sm.bar[m & (kRing - 1)], (m >> 4) & 1);
         }
 
-        // Consumer warp: Tjhung chain, J1_y ring and DY8, J1_x and DX8, compensated update and stores.
+        // Consumer warp: Tjhung chain, J1_x and DX8, compensated update and stores. The first 16
+        // rounds output nothing: they run the Tjhung chain only.
         template <int COMP, int NOISE>
         __device__ __forceinline__ void consumer(PairSmem& sm, float* __restrict__ phi_out,
                                                  __nv_bfloat16* residual, const StepParams& p, const Coef& k,
@@ -444,12 +464,6 @@ namespace amb
 
             float sxm[3][4], dxm[3][4], sxj[3][4], dxj[3][4];
             float jcy[4], jcx[4];
-            // xi_x and bf16 residual of the output row, fetched one round ahead (round 1 outputs row -7)
-            float xnx[4];
-            normals<NOISE>(p, k, injected, wrap_index(t.r0 - 16, ny), gcol, 1, xnx);
-            uint2 rnext = make_uint2(0u, 0u);
-            if constexpr (COMP == COMP_BF16)
-                rnext = *reinterpret_cast<const uint2*>(residual + (size_t)wrap_index(t.r0 - 16, ny) * nx + gcol);
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -457,167 +471,192 @@ namespace amb
 #pragma unroll
             for (int q = 0; q < 4; ++q) jcy[q] = jcx[q] = 0.f;
 
-            // Unrolled by 3 so the 3-row rings rotate by renaming.
-            for (int base = 0; base < total; base += 3)
+            // ---- Tjhung chain of round kl: J2 at row kl-1, divTj at row kl-2 (first needed: divTj of row 9)
+            const auto tjhung = [&](int kl) {
+                const float(*h)[kCols] = sm.hand[kl & 1];
+                float4 m4 = lds4(&h[0][4 * lane]);
+                float mL = __shfl_up_sync(0xffffffffu, m4.w, 1);
+                float mR = __shfl_down_sync(0xffffffffu, m4.x, 1);
+                float mm[6] = {mL, m4.x, m4.y, m4.z, m4.w, mR};
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                {
+                    sxm[0][q] = sxm[1][q]; sxm[1][q] = sxm[2][q];
+                    dxm[0][q] = dxm[1][q]; dxm[1][q] = dxm[2][q];
+                    sxm[2][q] = fmaf(0.1f, mm[q] + mm[q + 2], 0.3f * mm[q + 1]);
+                    dxm[2][q] = mm[q + 2] - mm[q];
+                }
+                float j2y[4], j2x[4];
+#pragma unroll
+                for (int q = 0; q < 4; q += 2)
+                {
+                    const auto P = [q](const float (&v)[4]) { return make_float2(v[q], v[q + 1]); };
+                    const float2 vy = __ffma2_rn(k.ndyp, sub2(P(sxm[2]), P(sxm[0])), P(jcy));
+                    const float2 vx = __ffma2_rn(k.jx3p, P(dxm[1]),
+                                                 __ffma2_rn(k.jx1p, __fadd2_rn(P(dxm[2]), P(dxm[0])), P(jcx)));
+                    j2y[q] = vy.x; j2y[q + 1] = vy.y;
+                    j2x[q] = vx.x; j2x[q + 1] = vx.y;
+                }
+                float4 cy4 = lds4(&h[1][4 * lane]), cx4 = lds4(&h[2][4 * lane]);
+                jcy[0] = cy4.x; jcy[1] = cy4.y; jcy[2] = cy4.z; jcy[3] = cy4.w;  // J_c at row kl
+                jcx[0] = cx4.x; jcx[1] = cx4.y; jcx[2] = cx4.z; jcx[3] = cx4.w;
+                float yL = __shfl_up_sync(0xffffffffu, j2y[3], 1);
+                float yR = __shfl_down_sync(0xffffffffu, j2y[0], 1);
+                float xL = __shfl_up_sync(0xffffffffu, j2x[3], 1);
+                float xR = __shfl_down_sync(0xffffffffu, j2x[0], 1);
+                float yy[6] = {yL, j2y[0], j2y[1], j2y[2], j2y[3], yR};
+                float xx[6] = {xL, j2x[0], j2x[1], j2x[2], j2x[3], xR};
+                float dtj[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                {
+                    sxj[0][q] = sxj[1][q]; sxj[1][q] = sxj[2][q];
+                    dxj[0][q] = dxj[1][q]; dxj[1][q] = dxj[2][q];
+                    sxj[2][q] = fmaf(0.1f, yy[q] + yy[q + 2], 0.3f * yy[q + 1]);
+                    dxj[2][q] = xx[q + 2] - xx[q];
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q += 2)
+                {
+                    const auto P = [q](const float (&v)[4]) { return make_float2(v[q], v[q + 1]); };
+                    float2 v = __fmul2_rn(k.tx1p, __fadd2_rn(P(dxj[0]), P(dxj[2])));
+                    v = __ffma2_rn(k.tx3p, P(dxj[1]), v);
+                    v = __ffma2_rn(k.dyInvp, sub2(P(sxj[2]), P(sxj[0])), v);
+                    dtj[q] = v.x; dtj[q + 1] = v.y;
+                }
+                sts4(&sm.dtj[(kl - 2) & (kDelay - 1)][4 * lane], dtj);
+            };
+
+            // Rounds 1..16: the chain only (unrolled by 3 so the 3-row rings rotate by renaming).
+            for (int base = 0; base < 15; base += 3)
             {
 #pragma unroll
-                for (int ph = 0; ph < 3; ++ph)
+                for (int ph = 1; ph <= 3; ++ph)
                 {
-                    const int kl = base + ph + 1;
+                    pair_sync(bar_id);
+                    tjhung(base + ph);
+                }
+            }
+            pair_sync(bar_id);
+            tjhung(16);
+
+            // Output rows: round kl (17 .. H+16) writes global row r0 + kl - 17 (never wraps). Its
+            // xi_x and bf16 residual are fetched one round ahead.
+            int grow = t.r0;
+            int mo = 9;        // mu_p ring slot of the output row ((kl - 8) mod 10)
+            float xnx[4];
+            normals<NOISE>(p, k, injected, grow, gcol, 1, xnx);
+            uint2 rnext = make_uint2(0u, 0u);
+            if constexpr (COMP == COMP_BF16)
+                rnext = *reinterpret_cast<const uint2*>(residual + (size_t)grow * nx + gcol);
+            const auto output = [&](int kl) {
+                const int lo = kl - 8;
+                const float(*h)[kCols] = sm.hand[kl & 1];
+                const float* mrow = sm.mup[mo];
+                mo = mo + 1 == kMupRing ? 0 : mo + 1;
+                float4 ml = lds4(&mrow[(4 * lane - 4) & (kCols - 1)]);
+                float4 mc = lds4(&mrow[4 * lane]);
+                float4 mr = lds4(&mrow[(4 * lane + 4) & (kCols - 1)]);
+                float mu[12] = {ml.x, ml.y, ml.z, ml.w, mc.x, mc.y, mc.z, mc.w, mr.x, mr.y, mr.z, mr.w};
+                float xi[4] = {xnx[0], xnx[1], xnx[2], xnx[3]};
+                // next round's xi_x and residual are fetched now, off this round's critical path
+                const int gnext = grow + 1 == ny ? 0 : grow + 1;
+                normals<NOISE>(p, k, injected, gnext, gcol, 1, xnx);
+                uint2 rv = rnext;
+                if constexpr (COMP == COMP_BF16)
+                    rnext = *reinterpret_cast<const uint2*>(residual + (size_t)gnext * nx + gcol);
+                float j1x[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                {
+                    float s = k.nx8[0] * (mu[q + 5] - mu[q + 3]);
+                    s = fmaf(k.nx8[1], mu[q + 6] - mu[q + 2], s);
+                    s = fmaf(k.nx8[2], mu[q + 7] - mu[q + 1], s);
+                    s = fmaf(k.nx8[3], mu[q + 8] - mu[q], s);
+                    j1x[q] = fmaf(k.mag, xi[q], s);
+                }
+                sts4(&sm.xch[4 * lane], j1x);
+                __syncwarp();
+                float4 jl = lds4(&sm.xch[(4 * lane - 4) & (kCols - 1)]);
+                float4 jr = lds4(&sm.xch[(4 * lane + 4) & (kCols - 1)]);
+                float jj[12] = {jl.x, jl.y, jl.z, jl.w, j1x[0], j1x[1], j1x[2], j1x[3], jr.x, jr.y, jr.z, jr.w};
+                __syncwarp();
+                float4 dt4 = lds4(&sm.dtj[lo & (kDelay - 1)][4 * lane]);
+                float4 dy4 = lds4(&h[3][4 * lane]);
+                const float dtv[4] = {dt4.x, dt4.y, dt4.z, dt4.w}, dyv[4] = {dy4.x, dy4.y, dy4.z, dy4.w};
+                float4 ph4 = lds4(&sm.phi[lo & (kRing - 1)][own]);
+                float fo[4] = {ph4.x, ph4.y, ph4.z, ph4.w};
+                const size_t gi = (size_t)grow * nx + gcol;
+                grow = gnext;
+                float rr[4] = {0.f, 0.f, 0.f, 0.f};
+                if constexpr (COMP == COMP_BF16)
+                {
+                    rr[0] = __uint_as_float(rv.x << 16);
+                    rr[1] = __uint_as_float(rv.x & 0xffff0000u);
+                    rr[2] = __uint_as_float(rv.y << 16);
+                    rr[3] = __uint_as_float(rv.y & 0xffff0000u);
+                }
+                float dx8[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                {
+                    float d = k.px8[0] * (jj[q + 5] - jj[q + 3]);
+                    d = fmaf(k.px8[1], jj[q + 6] - jj[q + 2], d);
+                    d = fmaf(k.px8[2], jj[q + 7] - jj[q + 1], d);
+                    dx8[q] = fmaf(k.px8[3], jj[q + 8] - jj[q], d);
+                }
+                // div = DX8 + (divTj + DY8); compensated update phi += y, y = -dt div - r,
+                // in column pairs: y = -F with F = fma(dt, div, r) (the same rounding),
+                // new phi = phi - F, new r = (new phi - phi) + F
+                float nf[4], nr[4];
+#pragma unroll
+                for (int q = 0; q < 4; q += 2)
+                {
+                    const auto P = [q](const float (&v)[4]) { return make_float2(v[q], v[q + 1]); };
+                    const float2 div = __fadd2_rn(P(dx8), __fadd2_rn(P(dtv), P(dyv)));
+                    float2 vf, vr;
+                    if constexpr (COMP == COMP_BF16)
+                    {
+                        const float2 F = __ffma2_rn(k.dtp, div, P(rr));
+                        vf = sub2(P(fo), F);
+                        vr = __fadd2_rn(sub2(vf, P(fo)), F);
+                    }
+                    else
+                    {
+                        vf = __ffma2_rn(k.ndtp, div, P(fo));
+                        vr = make_float2(0.f, 0.f);
+                    }
+                    nf[q] = vf.x; nf[q + 1] = vf.y;
+                    nr[q] = vr.x; nr[q + 1] = vr.y;
+                }
+                if (*reinterpret_cast<volatile int*>(&sm.abort))
+                    nf[0] = nf[1] = nf[2] = nf[3] = __int_as_float(0x7fc00000);
+                if (out_lane)
+                {
+                    *reinterpret_cast<float4*>(phi_out + gi) = make_float4(nf[0], nf[1], nf[2], nf[3]);
+                    if constexpr (COMP == COMP_BF16)
+                    {
+                        __nv_bfloat162 lo2 = __floats2bfloat162_rn(nr[0], nr[1]);
+                        __nv_bfloat162 hi2 = __floats2bfloat162_rn(nr[2], nr[3]);
+                        uint2 w;
+                        w.x = *reinterpret_cast<uint32_t*>(&lo2);
+                        w.y = *reinterpret_cast<uint32_t*>(&hi2);
+                        *reinterpret_cast<uint2*>(residual + gi) = w;
+                    }
+                }
+            };
+
+            // Rounds 17 .. H+16: chain and output (unrolled by 3, as the fill rounds).
+            for (int base = 16; base < total; base += 3)
+            {
+#pragma unroll
+                for (int ph = 1; ph <= 3; ++ph)
+                {
+                    const int kl = base + ph;
                     if (kl > total) break;
                     pair_sync(bar_id);
-                    const float(*h)[kCols] = sm.hand[kl & 1];
-                    // ---- Tjhung chain: J2 at row kl-1, divTj at row kl-2 (first needed: divTj of row 9)
-                    {
-                        float4 m4 = lds4(&h[0][4 * lane]);
-                        float mL = __shfl_up_sync(0xffffffffu, m4.w, 1);
-                        float mR = __shfl_down_sync(0xffffffffu, m4.x, 1);
-                        float mm[6] = {mL, m4.x, m4.y, m4.z, m4.w, mR};
-#pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                        {
-                            sxm[0][q] = sxm[1][q]; sxm[1][q] = sxm[2][q];
-                            dxm[0][q] = dxm[1][q]; dxm[1][q] = dxm[2][q];
-                            sxm[2][q] = fmaf(0.1f, mm[q] + mm[q + 2], 0.3f * mm[q + 1]);
-                            dxm[2][q] = mm[q + 2] - mm[q];
-                        }
-                        float j2y[4], j2x[4];
-#pragma unroll
-                        for (int q = 0; q < 4; q += 2)
-                        {
-                            const auto P = [q](const float (&v)[4]) { return make_float2(v[q], v[q + 1]); };
-                            const float2 vy = __ffma2_rn(k.ndyp, sub2(P(sxm[2]), P(sxm[0])), P(jcy));
-                            const float2 vx = __ffma2_rn(k.jx3p, P(dxm[1]),
-                                                         __ffma2_rn(k.jx1p, __fadd2_rn(P(dxm[2]), P(dxm[0])), P(jcx)));
-                            j2y[q] = vy.x; j2y[q + 1] = vy.y;
-                            j2x[q] = vx.x; j2x[q + 1] = vx.y;
-                        }
-                        float4 cy4 = lds4(&h[1][4 * lane]), cx4 = lds4(&h[2][4 * lane]);
-                        jcy[0] = cy4.x; jcy[1] = cy4.y; jcy[2] = cy4.z; jcy[3] = cy4.w;  // J_c at row kl
-                        jcx[0] = cx4.x; jcx[1] = cx4.y; jcx[2] = cx4.z; jcx[3] = cx4.w;
-                        float yL = __shfl_up_sync(0xffffffffu, j2y[3], 1);
-                        float yR = __shfl_down_sync(0xffffffffu, j2y[0], 1);
-                        float xL = __shfl_up_sync(0xffffffffu, j2x[3], 1);
-                        float xR = __shfl_down_sync(0xffffffffu, j2x[0], 1);
-                        float yy[6] = {yL, j2y[0], j2y[1], j2y[2], j2y[3], yR};
-                        float xx[6] = {xL, j2x[0], j2x[1], j2x[2], j2x[3], xR};
-                        float dtj[4];
-#pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                        {
-                            sxj[0][q] = sxj[1][q]; sxj[1][q] = sxj[2][q];
-                            dxj[0][q] = dxj[1][q]; dxj[1][q] = dxj[2][q];
-                            sxj[2][q] = fmaf(0.1f, yy[q] + yy[q + 2], 0.3f * yy[q + 1]);
-                            dxj[2][q] = xx[q + 2] - xx[q];
-                        }
-#pragma unroll
-                        for (int q = 0; q < 4; q += 2)
-                        {
-                            const auto P = [q](const float (&v)[4]) { return make_float2(v[q], v[q + 1]); };
-                            float2 v = __fmul2_rn(k.tx1p, __fadd2_rn(P(dxj[0]), P(dxj[2])));
-                            v = __ffma2_rn(k.tx3p, P(dxj[1]), v);
-                            v = __ffma2_rn(k.dyInvp, sub2(P(sxj[2]), P(sxj[0])), v);
-                            dtj[q] = v.x; dtj[q + 1] = v.y;
-                        }
-                        sts4(&sm.dtj[(kl - 2) & (kDelay - 1)][4 * lane], dtj);
-                    }
-                    // ---- output local row kl-8 (global r0 - 17 + kl); rounds before 17 run the same
-                    // code on rows nobody reads and store nothing
-                    {
-                        const int lo = kl - 8;
-                        const bool store = out_lane && kl >= 17;
-                        const float* mrow = sm.mup[(lo + kMupRing) % kMupRing];
-                        float4 ml = lds4(&mrow[(4 * lane - 4) & (kCols - 1)]);
-                        float4 mc = lds4(&mrow[4 * lane]);
-                        float4 mr = lds4(&mrow[(4 * lane + 4) & (kCols - 1)]);
-                        float mu[12] = {ml.x, ml.y, ml.z, ml.w, mc.x, mc.y, mc.z, mc.w, mr.x, mr.y, mr.z, mr.w};
-                        float xi[4] = {xnx[0], xnx[1], xnx[2], xnx[3]};
-                        const int grow = wrap_index(t.r0 - 9 + lo, ny);
-                        // next round's xi_x and residual are fetched now, off this round's critical path
-                        const int grow_next = wrap_index(t.r0 - 8 + lo, ny);
-                        normals<NOISE>(p, k, injected, grow_next, gcol, 1, xnx);
-                        uint2 rv = rnext;
-                        if constexpr (COMP == COMP_BF16)
-                            rnext = *reinterpret_cast<const uint2*>(residual + (size_t)grow_next * nx + gcol);
-                        float j1x[4];
-#pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                        {
-                            float s = k.nx8[0] * (mu[q + 5] - mu[q + 3]);
-                            s = fmaf(k.nx8[1], mu[q + 6] - mu[q + 2], s);
-                            s = fmaf(k.nx8[2], mu[q + 7] - mu[q + 1], s);
-                            s = fmaf(k.nx8[3], mu[q + 8] - mu[q], s);
-                            j1x[q] = fmaf(k.mag, xi[q], s);
-                        }
-                        sts4(&sm.xch[4 * lane], j1x);
-                        __syncwarp();
-                        float4 jl = lds4(&sm.xch[(4 * lane - 4) & (kCols - 1)]);
-                        float4 jr = lds4(&sm.xch[(4 * lane + 4) & (kCols - 1)]);
-                        float jj[12] = {jl.x, jl.y, jl.z, jl.w, j1x[0], j1x[1], j1x[2], j1x[3], jr.x, jr.y, jr.z, jr.w};
-                        __syncwarp();
-                        float4 dt4 = lds4(&sm.dtj[lo & (kDelay - 1)][4 * lane]);
-                        float4 dy4 = lds4(&h[3][4 * lane]);
-                        const float dtv[4] = {dt4.x, dt4.y, dt4.z, dt4.w}, dyv[4] = {dy4.x, dy4.y, dy4.z, dy4.w};
-                        float4 ph4 = lds4(&sm.phi[lo & (kRing - 1)][own]);
-                        float fo[4] = {ph4.x, ph4.y, ph4.z, ph4.w};
-                        const size_t gi = (size_t)grow * nx + gcol;
-                        float rr[4] = {0.f, 0.f, 0.f, 0.f};
-                        if constexpr (COMP == COMP_BF16)
-                        {
-                            rr[0] = __uint_as_float(rv.x << 16);
-                            rr[1] = __uint_as_float(rv.x & 0xffff0000u);
-                            rr[2] = __uint_as_float(rv.y << 16);
-                            rr[3] = __uint_as_float(rv.y & 0xffff0000u);
-                        }
-                        float dx8[4];
-#pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                        {
-                            float d = k.px8[0] * (jj[q + 5] - jj[q + 3]);
-                            d = fmaf(k.px8[1], jj[q + 6] - jj[q + 2], d);
-                            d = fmaf(k.px8[2], jj[q + 7] - jj[q + 1], d);
-                            dx8[q] = fmaf(k.px8[3], jj[q + 8] - jj[q], d);
-                        }
-                        // div = DX8 + (divTj + DY8); compensated update phi += y, y = -dt div - r,
-                        // in column pairs: y = -F with F = fma(dt, div, r) (the same rounding),
-                        // new phi = phi - F, new r = (new phi - phi) + F
-                        float nf[4], nr[4];
-#pragma unroll
-                        for (int q = 0; q < 4; q += 2)
-                        {
-                            const auto P = [q](const float (&v)[4]) { return make_float2(v[q], v[q + 1]); };
-                            const float2 div = __fadd2_rn(P(dx8), __fadd2_rn(P(dtv), P(dyv)));
-                            float2 vf, vr;
-                            if constexpr (COMP == COMP_BF16)
-                            {
-                                const float2 F = __ffma2_rn(k.dtp, div, P(rr));
-                                vf = sub2(P(fo), F);
-                                vr = __fadd2_rn(sub2(vf, P(fo)), F);
-                            }
-                            else
-                            {
-                                vf = __ffma2_rn(k.ndtp, div, P(fo));
-                                vr = make_float2(0.f, 0.f);
-                            }
-                            nf[q] = vf.x; nf[q + 1] = vf.y;
-                            nr[q] = vr.x; nr[q + 1] = vr.y;
-                        }
-                        if (*reinterpret_cast<volatile int*>(&sm.abort))
-                            nf[0] = nf[1] = nf[2] = nf[3] = __int_as_float(0x7fc00000);
-                        if (store)
-                        {
-                            *reinterpret_cast<float4*>(phi_out + gi) = make_float4(nf[0], nf[1], nf[2], nf[3]);
-                            if constexpr (COMP == COMP_BF16)
-                            {
-                                __nv_bfloat162 lo2 = __floats2bfloat162_rn(nr[0], nr[1]);
-                                __nv_bfloat162 hi2 = __floats2bfloat162_rn(nr[2], nr[3]);
-                                uint2 w;
-                                w.x = *reinterpret_cast<uint32_t*>(&lo2);
-                                w.y = *reinterpret_cast<uint32_t*>(&hi2);
-                                *reinterpret_cast<uint2*>(residual + gi) = w;
-                            }
-                        }
-                    }
+                    tjhung(kl);
+                    output(kl);
                 }
             }
         }

@@ -42,14 +42,24 @@ namespace amb
         }
     };
 
-    template <typename Real, int TY, int TX, int COMP>
-    __global__ void __launch_bounds__(256)
-    step_tile_kernel(const Real* __restrict__ phi_in, Real* __restrict__ phi_out,
-                     const __nv_bfloat16* comp_in, __nv_bfloat16* comp_out,  // may alias: each site reads/writes only its own
-                     StepParams p, const Canon<Real> k, int noise_mode, const Real* __restrict__ injected)
+    // Loads of the field a step reads. A persistent launch reads rows that other CTAs wrote
+    // earlier in the same launch: those loads go through L2 only (ld.global.cg), never a stale L1.
+    template <typename Real, bool COHERENT>
+    __device__ __forceinline__ Real load_field(const Real* p)
+    {
+        if constexpr (COHERENT) return __ldcg(p);
+        else return *p;
+    }
+
+    // One step of one TY x TX output tile (origin r0, c0): the whole body of the tile kernel.
+    template <typename Real, int TY, int TX, int COMP, bool COHERENT>
+    __device__ __forceinline__ void tile_step(const Real* __restrict__ phi_in, Real* __restrict__ phi_out,
+                                              const __nv_bfloat16* comp_in, __nv_bfloat16* comp_out,
+                                              const StepParams& p, const Canon<Real>& k, int noise_mode,
+                                              const Real* __restrict__ injected, int r0, int c0,
+                                              unsigned char* smem_raw)
     {
         using G = TileGeom<TY, TX>;
-        extern __shared__ __align__(16) unsigned char smem_raw[];
         Real* PHI = reinterpret_cast<Real*>(smem_raw);
         Real* MUP = PHI + G::LY * G::LX;
         Real* MUA = MUP + G::MY * G::MX;
@@ -59,7 +69,6 @@ namespace amb
         Real* J1X = J1Y + G::PY * TX;
 
         const int ny = p.ny, nx = p.nx;
-        const int r0 = blockIdx.y * TY, c0 = blockIdx.x * TX;
         const int tid = threadIdx.x, nthr = blockDim.x;
 
         // Load phi(t) with a 9-site periodic halo.
@@ -68,7 +77,7 @@ namespace amb
             int i = e / G::LX, j = e - i * G::LX;
             int gr = wrap_index(r0 + i - G::H, ny);
             int gc = wrap_index(c0 + j - G::H, nx);
-            PHI[e] = phi_in[(size_t)gr * nx + gc];
+            PHI[e] = load_field<Real, COHERENT>(phi_in + (size_t)gr * nx + gc);
         }
         __syncthreads();
 
@@ -191,13 +200,101 @@ namespace amb
             const size_t gi = (size_t)gr * nx + gc;
             if constexpr (COMP == COMP_BF16)
             {
-                float r = __bfloat162float(comp_in[gi]);
+                float r = __bfloat162float(load_field<__nv_bfloat16, COHERENT>(comp_in + gi));
                 phi_out[gi] = canon_update_comp(f, dx8, divtj, dy8, r, k);
                 comp_out[gi] = __float2bfloat16_rn(r);
             }
             else
             {
                 phi_out[gi] = canon_update(f, dx8, divtj, dy8, k);
+            }
+        }
+    }
+
+    // One step, one tile per CTA (grid = tiles).
+    template <typename Real, int TY, int TX, int COMP, int NT>
+    __global__ void __launch_bounds__(NT)
+    step_tile_kernel(const Real* __restrict__ phi_in, Real* __restrict__ phi_out,
+                     const __nv_bfloat16* comp_in, __nv_bfloat16* comp_out,  // may alias: each site reads/writes only its own
+                     StepParams p, const Canon<Real> k, int noise_mode, const Real* __restrict__ injected)
+    {
+        extern __shared__ __align__(16) unsigned char smem_raw[];
+        tile_step<Real, TY, TX, COMP, false>(phi_in, phi_out, comp_in, comp_out, p, k, noise_mode, injected,
+                                             blockIdx.y * TY, blockIdx.x * TX, smem_raw);
+    }
+
+    constexpr long long kGridBarrierSpin = 1ll << 24;  // ~1 s of polling at >= 64 ns per poll
+
+    // Bounded grid-wide barrier of a cooperative launch: every CTA adds one arrival to *count and
+    // waits until `target` arrivals are there. Returns false (and sets *error) if the wait gave up.
+    __device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned target, int* error, int* ok_smem)
+    {
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            __threadfence();
+            atomicAdd(count, 1u);
+            bool done = false;
+            for (long long it = 0; it < kGridBarrierSpin; ++it)
+            {
+                if (*reinterpret_cast<volatile unsigned*>(count) >= target)
+                {
+                    done = true;
+                    break;
+                }
+                __nanosleep(64);
+            }
+            if (!done) atomicOr(error, 1);
+            __threadfence();
+            *ok_smem = done ? 1 : 0;
+        }
+        __syncthreads();
+        return *ok_smem != 0;
+    }
+
+    // nsteps steps in one cooperative launch: each CTA owns tiles blockIdx.x, +gridDim.x, ... for
+    // the whole launch, and a bounded grid barrier separates the steps. Step s reads buf[s % 2]
+    // and writes buf[(s + 1) % 2]. The per-site arithmetic is the tile kernel's (tile_step), so
+    // the result is bitwise that of nsteps single-step launches. If a barrier gives up, the CTA
+    // fills its tiles of both buffers with NaN (caught by the finite check) and leaves.
+    template <typename Real, int TY, int TX, int COMP, int NT>
+    __global__ void __launch_bounds__(NT)
+    step_tile_persistent_kernel(Real* buf0, Real* buf1, __nv_bfloat16* comp, StepParams p, const Canon<Real> k,
+                                int noise_mode, const Real* __restrict__ injected, int nsteps, unsigned* count,
+                                int* error)
+    {
+        extern __shared__ __align__(16) unsigned char smem_raw[];
+        __shared__ int ok;
+        const int tx = (p.nx + TX - 1) / TX, ty = (p.ny + TY - 1) / TY;
+        const int ntiles = tx * ty;
+        const size_t plane = (size_t)p.ny * p.nx;
+        const int64_t step0 = p.step;
+        for (int s = 0; s < nsteps; ++s)
+        {
+            const Real* in = (s & 1) ? buf1 : buf0;
+            Real* out = (s & 1) ? buf0 : buf1;
+            p.step = step0 + s;
+            const Real* inj = injected ? injected + (size_t)s * 2 * plane : nullptr;
+            for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+            {
+                tile_step<Real, TY, TX, COMP, true>(in, out, comp, comp, p, k, noise_mode, inj, (tile / tx) * TY,
+                                                    (tile % tx) * TX, smem_raw);
+                __syncthreads();
+            }
+            if (s + 1 < nsteps && !grid_barrier(count, unsigned(s + 1) * gridDim.x, error, &ok))
+            {
+                const Real nan = Real(__int_as_float(0x7fc00000));
+                for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+                    for (int e = threadIdx.x; e < TY * TX; e += blockDim.x)
+                    {
+                        const int r = (tile / tx) * TY + e / TX, c = (tile % tx) * TX + e % TX;
+                        if (r < p.ny && c < p.nx)
+                        {
+                            buf0[(size_t)r * p.nx + c] = nan;
+                            buf1[(size_t)r * p.nx + c] = nan;
+                        }
+                    }
+                return;
             }
         }
     }

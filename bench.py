@@ -73,7 +73,10 @@ def parse_args(argv=None):
                     help="profiling: N forward passes of the learned stepper's network on a 512^2 field")
     ap.add_argument("--seg-rows", type=int, default=0,
                     help="with --kernel sliding: row-segment height (e.g. the autotuner's choice, for profiling)")
-    ap.add_argument("--pairs", type=int, default=0, help="with --kernel sliding: warp pairs per CTA")
+    ap.add_argument("--pairs", type=int, default=0,
+                    help="with --kernel sliding: warp pairs per CTA; with --kernel tile: 256-thread groups per CTA")
+    ap.add_argument("--persistent", action="store_true",
+                    help="with --kernel tile: all steps of a run in one cooperative launch")
     ap.add_argument("--launches", type=int, default=0,
                     help="profiling driver: run this many bare step launches through the C ABI and exit")
     ap.add_argument("--sweep", action="store_true",
@@ -333,8 +336,11 @@ def run_ours(args, w, rank, world, dist):
     model = Model(w["a"], w["b"], w["c"], w["kappa"], w["lamb"], w["zeta"], w["T"])
     field = initial_field(w, rank)
     sites = w["ny"] * w["nx"]
-    launch = ({"seg_rows": args.seg_rows, "pairs_per_cta": args.pairs}
-              if args.kernel == "sliding" and (args.seg_rows or args.pairs) else None)
+    launch = None
+    if args.kernel == "sliding" and (args.seg_rows or args.pairs):
+        launch = {"seg_rows": args.seg_rows, "pairs_per_cta": args.pairs}
+    elif args.kernel == "tile" and (args.pairs or args.persistent):
+        launch = {"pairs_per_cta": args.pairs, "persistent": args.persistent}
     sim = Integrator(field, stencil, model, precision=args.precision, seed=1000 + rank, kernel=args.kernel,
                      launch=launch)
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
@@ -445,7 +451,8 @@ def run_launches(args, w):
                             args.launches, None, stream, None)
     else:
         res = torch.zeros(a.shape, dtype=torch.int16, device="cuda") if args.precision == "f32c" else None
-        cfg = N.amb_kernel_config({"auto": 0, "tile": 1, "sliding": 2}[args.kernel], args.seg_rows, args.pairs, 0)
+        cfg = N.amb_kernel_config({"auto": 0, "tile": 1, "sliding": 2}[args.kernel], args.seg_rows, args.pairs,
+                                  N.AMB_FLAG_PERSISTENT if args.persistent else 0)
         rc = L.amb_step_f32_ex(ctypes.byref(s), ctypes.byref(m), 1, w["ny"], w["nx"], a.data_ptr(), b.data_ptr(),
                                res.data_ptr() if res is not None else None, 0, args.launches, None, ctypes.byref(cfg),
                                stream, None)

@@ -80,15 +80,22 @@ typedef struct amb_model
 #define AMB_KERNEL_TILE 1    /* shared-memory tile kernel, any grid */
 #define AMB_KERNEL_SLIDING 2 /* warp-pair sliding FP32 kernel (ncols % 4 == 0, ncols >= 112, 16-byte aligned) */
 
-/* Explicit kernel configuration for amb_step_f32_ex (zeros mean defaults).
- * seg_rows: rows per warp-pair task of the sliding kernel; pairs_per_cta: 1, 2 or 4. */
+/* Explicit kernel configuration for amb_step_f32_ex / amb_step_f64_ex (zeros mean defaults).
+ * seg_rows: rows per warp-pair task of the sliding kernel.
+ * pairs_per_cta: sliding kernel: warp pairs per CTA (1, 2 or 4); tile kernel: groups of 256
+ *   threads per CTA (1, 2 or 4).
+ * flags: AMB_FLAG_PERSISTENT (tile kernel): all nsteps of the call in one cooperative launch,
+ *   a grid-wide barrier between the steps (for grids too small to fill the GPU, where a launch
+ *   per step costs more than the step; ignored while the stream is being captured). The
+ *   results are bitwise those of one launch per step. */
 typedef struct amb_kernel_config
 {
     int kernel;
     int seg_rows;
     int pairs_per_cta;
-    int reserved;
+    int flags;
 } amb_kernel_config;
+#define AMB_FLAG_PERSISTENT 1
 
 /* Number of FP64 planes written by amb_terms_*: mu_p, mu_a, J_p(y,x), J_l(y,x), J_c(y,x), J_r(y,x). */
 #define AMB_NTERMS 10
@@ -147,6 +154,11 @@ int amb_integrator_get_shape(const amb_integrator* h, int* nrows, int* ncols, in
 int amb_step_f64(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows, int ncols,
                  double* field, double* spare, int64_t step0, int nsteps, const double* injected_noise,
                  void* stream, int* result_in_spare);
+/* amb_step_f64 with an explicit tile-kernel configuration (kernel AMB_KERNEL_AUTO or
+ * AMB_KERNEL_TILE; pairs_per_cta and flags as in amb_kernel_config; NULL = defaults). */
+int amb_step_f64_ex(const amb_stencil* stencil, const amb_model* model, uint64_t seed, int nrows, int ncols,
+                    double* field, double* spare, int64_t step0, int nsteps, const double* injected_noise,
+                    const amb_kernel_config* config, void* stream, int* result_in_spare);
 /* FP32 storage. residual: NULL for plain FP32 (AMB_F32), else a device plane of
  * nrows*ncols bf16 words updated in place (AMB_F32C; zero it before the first step).
  * kernel: AMB_KERNEL_*. */

@@ -24,7 +24,8 @@ def native():
     return N
 
 
-def run_f32(field, p: Params, nsteps, *, kernel=1, seg_rows=0, pairs=0, comp=True, seed=7, injected=None, step0=0):
+def run_f32(field, p: Params, nsteps, *, kernel=1, seg_rows=0, pairs=0, comp=True, seed=7, injected=None, step0=0,
+            flags=0):
     import torch
     N = native()
     ny, nx = field.shape
@@ -34,7 +35,7 @@ def run_f32(field, p: Params, nsteps, *, kernel=1, seg_rows=0, pairs=0, comp=Tru
     inj = None if injected is None else torch.from_numpy(injected.astype(np.float32)).cuda()
     s = N.amb_stencil(p.dt, p.dx, p.dy)
     m = N.amb_model(p.a, p.b, p.c, p.kappa, p.lamb, p.zeta, p.T)
-    cfg = N.amb_kernel_config(kernel, seg_rows, pairs, 0)
+    cfg = N.amb_kernel_config(kernel, seg_rows, pairs, flags)
     flag = ctypes.c_int(0)
     rc = N.lib().amb_step_f32_ex(ctypes.byref(s), ctypes.byref(m), seed, ny, nx, a.data_ptr(), b.data_ptr(),
                                  res.data_ptr() if comp else None, step0, nsteps,
@@ -184,3 +185,46 @@ def test_kernels_match_pinned_bits():
         want = pins[M.case_name("sliding", shape, comp, T)]
         for kernel in (1, 2):
             assert M.run_case(kernel, shape, comp, T) == want, (kernel, shape, comp, T)
+
+
+# ------------------------------------------ tile kernel: thread groups and persistent launches
+
+@pytest.mark.parametrize("shape", [(256, 256), (100, 72), (33, 17), (512, 512), (64, 1000)])
+@pytest.mark.parametrize("groups", [1, 2, 4])
+def test_tile_thread_groups_and_persistent_launch_are_bitwise(shape, groups):
+    """256/512/1024 threads per CTA, one launch per step or all steps in one cooperative launch
+    (grid barrier between steps): bitwise the single-step 256-thread result, for odd and even
+    step counts (the result ends in either buffer)."""
+    field = initial(shape, seed=shape[1])
+    p = Params(T=0.05, **AMB)
+    for comp in (False, True):
+        for nsteps in (12, 13):
+            ref = run_f32(field, p, nsteps, kernel=1, comp=comp)
+            assert np.array_equal(run_f32(field, p, nsteps, kernel=1, pairs=groups, comp=comp), ref)
+            assert np.array_equal(run_f32(field, p, nsteps, kernel=1, pairs=groups, flags=1, comp=comp), ref)
+
+
+def test_tile_persistent_injected_noise_and_fp64():
+    """The persistent launch with host-injected noise (one pair of planes per step) and in FP64:
+    bitwise one launch per step."""
+    import torch
+    N = native()
+    rng = np.random.default_rng(21)
+    field = initial((96, 160), seed=21)
+    noise = rng.standard_normal((7, 2, 96, 160))
+    p = Params(T=0.05, **AMB)
+    ref = run_f32(field, p, 7, kernel=1, comp=True, injected=noise)
+    assert np.array_equal(run_f32(field, p, 7, kernel=1, comp=True, injected=noise, flags=1, pairs=2), ref)
+    s = N.amb_stencil(p.dt, p.dx, p.dy)
+    m = N.amb_model(p.a, p.b, p.c, p.kappa, p.lamb, p.zeta, p.T)
+    stream = torch.cuda.current_stream().cuda_stream
+    outs = []
+    for cfg in (None, N.amb_kernel_config(1, 0, 2, N.AMB_FLAG_PERSISTENT)):
+        a = torch.from_numpy(field.copy()).cuda()
+        b = torch.empty_like(a)
+        flag = ctypes.c_int(0)
+        rc = N.lib().amb_step_f64_ex(ctypes.byref(s), ctypes.byref(m), 5, 96, 160, a.data_ptr(), b.data_ptr(), 0, 9,
+                                     None, ctypes.byref(cfg) if cfg is not None else None, stream, ctypes.byref(flag))
+        assert rc == 0, N.last_error()
+        outs.append((b if flag.value else a).cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
