@@ -82,6 +82,31 @@ def mean_wavenumber(k, S) -> float:
     return float(simpson(k[m] * S[m], x=k[m]) / simpson(S[m], x=k[m]))
 
 
+def peak_wavenumber(k, S, frac: float = 0.5) -> float:
+    """Sub-bin position of the maximum of a binned S(k): the vertex of the least-squares
+    parabola through the contiguous bins around the largest one whose S is at least ``frac``
+    of it (at least the three bins centred on the maximum). Falls back to the largest bin's
+    k if the fit has no maximum inside those bins."""
+    k = np.asarray(k, dtype=np.float64)
+    S = np.asarray(S, dtype=np.float64)
+    m = np.isfinite(S)
+    k, S = k[m], S[m]
+    i = int(np.argmax(S))
+    lo, hi = i, i
+    while lo > 0 and S[lo - 1] >= frac * S[i]:
+        lo -= 1
+    while hi < len(S) - 1 and S[hi + 1] >= frac * S[i]:
+        hi += 1
+    lo, hi = max(0, min(lo, i - 1)), min(len(S) - 1, max(hi, i + 1))
+    if hi - lo < 2:
+        return float(k[i])
+    c2, c1, _ = np.polyfit(k[lo:hi + 1] - k[i], S[lo:hi + 1], 2)
+    if c2 >= 0:
+        return float(k[i])
+    v = -c1 / (2 * c2) + k[i]
+    return float(v) if k[lo] <= v <= k[hi] else float(k[i])
+
+
 def label_droplets(field, threshold: float | None = None):
     """(labels, count): periodic 4-connected components of {phi > threshold} (threshold
     defaults to the field mean). labels is a device int32 tensor (-1 = background)."""

@@ -940,17 +940,29 @@ def _timed(fn):
     return time.perf_counter() - t0
 
 
+def _mean_rel_err(learned, plain) -> tuple[float, float]:
+    """Signed relative difference of the means (learned - plain) / plain and its standard error
+    (sample standard deviations, independent arms)."""
+    learned, plain = np.asarray(learned, dtype=np.float64), np.asarray(plain, dtype=np.float64)
+    se2 = sum(float(v.std(ddof=1)) ** 2 / len(v) for v in (plain, learned) if len(v) > 1)
+    return float((learned.mean() - plain.mean()) / plain.mean()), float(np.sqrt(se2) / plain.mean())
+
+
 def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: int | None = None, seed: int = 0,
-                       check_every: int = 40, tol: float = 0.5, plain_seeds=(1, 2, 3), residual_sigma: float = 2.0,
-                       filter_noise: bool = True, atol: float = 0.0, learned_runs: int = 3,
-                       max_check_every: int | None = 320) -> dict:
+                       check_every: int = 40, tol: float = 0.5, plain_seeds=tuple(range(1, 11)),
+                       residual_sigma: float = 2.0, filter_noise: bool = True, atol: float = 0.0,
+                       learned_runs: int = 10, max_check_every: int | None = 320, plain_launch: dict | None = None) -> dict:
     """Time to ``t_end`` and end-state statistics of the learned stepper against the plain
     FP32 integrator (the faster of the Integrator and a one-replica CUDA-graph ensemble)
-    from the same initial field: S(k) mean wavenumber (the reference notebook's
-    definition), droplet count, mass. The plain run is repeated with ``plain_seeds`` and the
-    learned run with ``learned_runs`` noise seeds (``seed``, ``seed + 1``, ...): the error is
-    that of the learned mean against the plain mean, the speed-up that of the fastest runs."""
-    from .analysis import count_droplets, mean_wavenumber, structure_factor
+    from the same initial field: the position of the S(k) peak (sub-bin estimate,
+    ``analysis.peak_wavenumber``) and the S(k) mean wavenumber (both over the reference
+    notebook's binned S(k)), droplet count, mass. The plain run is repeated with
+    ``plain_seeds`` and the learned run with ``learned_runs`` noise seeds (``seed``, ``seed +
+    1``, ...): each error is that of the learned mean against the plain mean with its standard
+    error, the speed-up that of the fastest runs. ``plain_launch`` names the plain
+    integrator's launch shape (``Integrator(kernel="tile", launch=...)``); by default the
+    autotuner picks it."""
+    from .analysis import count_droplets, mean_wavenumber, peak_wavenumber, structure_factor
     stencil, model = Stencil(stencil), Model(model)
     K = int(K if K is not None else getattr(net, "K", 50))
     nsteps = int(round(t_end / stencil.dt))
@@ -960,7 +972,8 @@ def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: 
            "check_every": check_every, "max_check_every": max_check_every, "residual_sigma": residual_sigma,
            "filter_noise": filter_noise, "plain": []}
     probe = max(1, min(nsteps, 20000))
-    sim = Integrator(field, stencil, model, precision="f32", seed=0)
+    plain_kw = {"kernel": "tile", "launch": plain_launch} if plain_launch else {}
+    sim = Integrator(field, stencil, model, precision="f32", seed=0, **plain_kw)
     t_int = _timed(lambda: sim.run(probe))
     res["plain_kernel_config"] = getattr(sim, "kernel_config", None)
     del sim
@@ -977,14 +990,14 @@ def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: 
             f = ens.field(0)
             ens.close()
         else:
-            sim = Integrator(field, stencil, model, precision="f32", seed=sd)
+            sim = Integrator(field, stencil, model, precision="f32", seed=sd, **plain_kw)
             sec = _timed(lambda: sim.run(nsteps))
             f = sim.field
             del sim
         k, S, _ = structure_factor(f, stencil.dx, stencil.dy, phi0=phi0)
         res["plain"].append({"seconds": sec, "seed": sd, "k_avg": mean_wavenumber(k, S),
-                             "k_peak": float(k[np.nanargmax(S)]), "droplets": count_droplets(f, phi0),
-                             "mass_drift": float(f.sum() - field.sum())})
+                             "k_peak": peak_wavenumber(k, S), "k_peak_bin": float(k[np.nanargmax(S)]),
+                             "droplets": count_droplets(f, phi0), "mass_drift": float(f.sum() - field.sum())})
     res["learned_runs"] = []
     for sd in range(seed, seed + max(1, int(learned_runs))):
         st = LearnedStepper(net, field, stencil, model, K=K, seed=sd, check_every=check_every, tol=tol,
@@ -995,7 +1008,8 @@ def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: 
         f = st.field
         k, S, _ = structure_factor(f, stencil.dx, stencil.dy, phi0=phi0)
         res["learned_runs"].append({"seconds": sec, "seed": sd, "k_avg": mean_wavenumber(k, S),
-                                    "k_peak": float(k[np.nanargmax(S)]), "droplets": count_droplets(f, phi0),
+                                    "k_peak": peak_wavenumber(k, S), "k_peak_bin": float(k[np.nanargmax(S)]),
+                                    "droplets": count_droplets(f, phi0),
                                     "mass_q_drift": st.mass_q() - m0, "macro_steps": st.macro_steps,
                                     "learned_macro_steps": st.learned_steps, "fallback_spans": st.fallback_spans,
                                     "checks": st.checks, "max_residual": max(st.residuals) if st.residuals else None,
@@ -1009,16 +1023,30 @@ def compare_with_plain(net: FluxNet, field, stencil, model, *, t_end: float, K: 
     res["plain_k_avg_std"] = float(plain_k.std())
     res["learned_k_avg_mean"] = float(learned_k.mean())
     res["learned_k_avg_std"] = float(learned_k.std())
-    res["k_avg_rel_err"] = abs(learned_k.mean() - plain_k.mean()) / plain_k.mean()
-    # standard error of that difference of means (sample standard deviations)
-    se2 = sum(float(v.std(ddof=1)) ** 2 / len(v) for v in (plain_k, learned_k) if len(v) > 1)
-    res["k_avg_rel_err_se"] = float(np.sqrt(se2)) / float(plain_k.mean())
+    err, se = _mean_rel_err(learned_k, plain_k)
+    res["k_avg_rel_err"], res["k_avg_rel_err_se"] = abs(err), se
+    for key in ("k_peak", "droplets"):
+        err, se = _mean_rel_err([r[key] for r in runs], [p[key] for p in res["plain"]])
+        res[f"{key}_rel_err"], res[f"{key}_rel_err_se"] = err, se
+        res[f"plain_{key}_mean"] = float(np.mean([p[key] for p in res["plain"]]))
+        res[f"learned_{key}_mean"] = float(np.mean([r[key] for r in runs]))
     res["plain_seconds_min"] = float(min(p["seconds"] for p in res["plain"]))
     res["learned_seconds_min"] = float(min(r["seconds"] for r in runs))
     res["learned_fallback_spans"] = int(sum(r["fallback_spans"] for r in runs))
     res["learned_mass_q_drift_max"] = int(max(abs(r["mass_q_drift"]) for r in runs))
     res["speedup"] = res["plain_seconds_min"] / res["learned_seconds_min"]
     return res
+
+
+def _parse_launch(text: str) -> dict | None:
+    """'pairs_per_cta=2,persistent=1' -> {"pairs_per_cta": 2, "persistent": True}; '' -> None."""
+    if not text:
+        return None
+    out = {}
+    for item in text.split(","):
+        key, val = item.split("=")
+        out[key.strip()] = bool(int(val)) if key.strip() == "persistent" else int(val)
+    return out
 
 
 def _main(argv=None) -> int:
@@ -1050,7 +1078,10 @@ def _main(argv=None) -> int:
     c.add_argument("--temperature", type=float, default=0.05)
     c.add_argument("--residual-sigma", type=float, default=2.0)
     c.add_argument("--no-noise-filter", action="store_true")
-    c.add_argument("--plain-seeds", default="1,2,3")
+    c.add_argument("--plain-seeds", default=",".join(str(v) for v in range(1, 11)))
+    c.add_argument("--learned-runs", type=int, default=10)
+    c.add_argument("--plain-launch", default="",
+                   help="plain integrator launch shape, e.g. 'pairs_per_cta=2,persistent=1' (tile kernel)")
     c.add_argument("--atol", type=float, default=0.0)
     a = ap.parse_args(argv)
     if a.cmd == "train":
@@ -1072,7 +1103,8 @@ def _main(argv=None) -> int:
                              check_every=a.check_every, max_check_every=a.max_check_every, tol=a.tol,
                              residual_sigma=a.residual_sigma,
                              filter_noise=not a.no_noise_filter, atol=a.atol,
-                             plain_seeds=tuple(int(v) for v in a.plain_seeds.split(",")))
+                             plain_seeds=tuple(int(v) for v in a.plain_seeds.split(",")),
+                             learned_runs=a.learned_runs, plain_launch=_parse_launch(a.plain_launch))
     print(json.dumps(res))
     return 0
 

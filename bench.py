@@ -66,6 +66,9 @@ def parse_args(argv=None):
     ap.add_argument("--learned", action="store_true",
                     help="learned coarse stepper vs plain FP32: time to --t-end on a 512^2 AMB+ field")
     ap.add_argument("--t-end", type=float, default=1000.0)
+    ap.add_argument("--learned-seeds", type=int, default=10, help="with --learned: noise seeds per arm")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="leave the learned-vs-plain comparison (one seed per arm) out of the default bench line")
     ap.add_argument("--weights", default=os.path.join(PKG, "activemodelbplus", "weights", "fluxnet_k50.npz"))
     ap.add_argument("--learned-steps", type=int, default=0,
                     help="time N macro steps of the learned stepper on the 512^2 field (after 40 untimed)")
@@ -431,6 +434,11 @@ def run_ours(args, w, rank, world, dist):
     if not args.no_cpu and world == 1:
         line["cpu_baseline"] = cpu_baseline(w)
         line["reference_gpu"] = reference_gpu_baseline(w)
+    if not args.no_learned and world == 1 and os.path.exists(args.weights):
+        # the metric's second half: learned surrogate vs plain FP32 time to t = 10^3 at 512^2
+        # (one noise seed per arm here; `bench.py --learned` runs ten per arm)
+        res, _ = learned_comparison(args, 1)
+        line["learned_time_to_t"] = learned_summary(res)
     print(json.dumps(line), flush=True)
 
 
@@ -595,13 +603,14 @@ def run_learned_steps(args):
                       "euler_steps_per_macro_step": net.K, "fallback_spans": st.fallback_spans}))
 
 
-def run_learned(args):
-    """Learned coarse stepper (K = 50 Euler steps per network evaluation) against the plain
+def learned_comparison(args, seeds: int):
+    """The learned coarse stepper (K = 50 Euler steps per network evaluation) against the plain
     FP32 integrator, both from the same seeded 512^2 field (phi = -0.4 + 0.01 N(0,1), numpy seed
-    0; a=-0.25 b=0 c=0.25 kappa=1 lambda=-1 zeta=-4 T=0.05, dt=1e-3) to t_end: wall time of each
-    (CUDA-synchronised; the fastest of the repeated runs of each), the S(k) mean wavenumber of
-    the end states (each over three noise seeds), droplet counts and the learned runs' exact
-    fixed-point mass drift."""
+    0; a=-0.25 b=0 c=0.25 kappa=1 lambda=-1 zeta=-4 T=0.05, dt=1e-3) to t_end, ``seeds`` noise
+    seeds per arm: wall time of each (CUDA-synchronised; the fastest run of each arm counts), the
+    S(k) peak position (sub-bin) and mean wavenumber and the droplet count of the end states
+    (learned mean against plain mean, with standard errors), and the learned runs' exact
+    fixed-point mass drift. Returns (compare record, clocks summary)."""
     import torch
     from activemodelbplus import learned as L
     from activemodelbplus.integrator import Model, Stencil
@@ -609,22 +618,38 @@ def run_learned(args):
     field = -0.4 + 0.01 * np.random.default_rng(0).standard_normal((512, 512))
     model = Model(a=-0.25, b=0, c=0.25, kappa=1, lamb=-1, zeta=-4, T=0.05)
     with ClockSampler(torch.cuda.current_device()) as clocks:
-        res = L.compare_with_plain(net, field, Stencil(1e-3, 1, 1), model, t_end=args.t_end, residual_sigma=2.0)
+        res = L.compare_with_plain(net, field, Stencil(1e-3, 1, 1), model, t_end=args.t_end, residual_sigma=2.0,
+                                   plain_seeds=tuple(range(1, seeds + 1)), learned_runs=seeds)
+    return res, clocks.summary()
+
+
+def learned_summary(res) -> dict:
+    """The bench-line digest of a learned-vs-plain comparison record."""
+    return {"workload": f"512^2 AMB+ (zeta=-4, lambda=-1, T=0.05) to t={res['t_end']:g}, K=50",
+            "speedup": res["speedup"], "plain_seconds": res["plain_seconds_min"],
+            "learned_seconds": res["learned_seconds_min"], "plain_path": res["plain_path"],
+            "plain_kernel_config": res.get("plain_kernel_config"), "seeds_per_arm": len(res["plain"]),
+            "k_peak_plain": res["plain_k_peak_mean"], "k_peak_learned": res["learned_k_peak_mean"],
+            "k_peak_rel_err": res["k_peak_rel_err"], "k_peak_rel_err_se": res["k_peak_rel_err_se"],
+            "k_avg_rel_err": res["k_avg_rel_err"], "k_avg_rel_err_se": res["k_avg_rel_err_se"],
+            "droplets_plain": res["plain_droplets_mean"], "droplets_learned": res["learned_droplets_mean"],
+            "droplets_rel_err": res["droplets_rel_err"], "droplets_rel_err_se": res["droplets_rel_err_se"],
+            "mass_q_drift_learned_max": res["learned_mass_q_drift_max"],
+            "fallback_spans": res["learned_fallback_spans"],
+            "max_residual": max(r["max_residual"] for r in res["learned_runs"])}
+
+
+def run_learned(args):
+    """``--learned``: the learned-vs-plain comparison with --learned-seeds seeds per arm, as one
+    JSON line whose value is the speed-up."""
+    res, clocks = learned_comparison(args, args.learned_seeds)
     out = {"metric": f"learned vs plain FP32 time to t={args.t_end:g} (512^2 AMB+), speed-up", "value": res["speedup"],
            "unit": "x", "higher_is_better": True, "n_gpus": 1, "dtype": "bf16 network / int32 fixed-point field",
            "data": "synthetic", "config": {"workload": "learned_time_to_t", "size": 512, "K": 50,
                                            "t_end": args.t_end, "check_every": res["check_every"],
                                            "max_check_every": res["max_check_every"], "tol": res["tol"]},
-           "plain_seconds": res["plain_seconds_min"], "learned_seconds": res["learned_seconds_min"],
-           "plain_path": res["plain_path"], "k_avg_plain_mean": res["plain_k_avg_mean"],
-           "k_avg_plain_std": res["plain_k_avg_std"], "k_avg_learned_mean": res["learned_k_avg_mean"],
-           "k_avg_learned_std": res["learned_k_avg_std"],
-           "k_avg_rel_err": res["k_avg_rel_err"], "k_avg_rel_err_se": res["k_avg_rel_err_se"], "droplets_plain": [p_["droplets"] for p_ in res["plain"]],
-           "droplets_learned": [r["droplets"] for r in res["learned_runs"]],
-           "mass_q_drift_learned_max": res["learned_mass_q_drift_max"],
-           "learned_macro_steps": [r["learned_macro_steps"] for r in res["learned_runs"]],
-           "fallback_spans": res["learned_fallback_spans"], "checks": [r["checks"] for r in res["learned_runs"]],
-           "max_residual": max(r["max_residual"] for r in res["learned_runs"]), "clocks": clocks.summary()}
+           **learned_summary(res),
+           "runs_plain": res["plain"], "runs_learned": res["learned_runs"], "clocks": clocks}
     print(json.dumps(out), flush=True)
 
 

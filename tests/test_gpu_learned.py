@@ -298,12 +298,10 @@ def test_linear_macro_step_matches_the_propagator():
     assert s.mass_q() == int(np.rint(start * L.FIX).astype(np.int64).sum())
 
 
-def test_training_gains_over_untrained_and_naive_coarse_step():
+def test_training_gains_over_untrained():
     """A short training run on plain-integrator pairs: the trained flux predicts the
-    deterministic 50-step increment far better than the untrained network and than one
-    explicit Euler step of size 50 dt (the method without the network)."""
+    deterministic 50-step increment far better than the untrained network."""
     torch, L, N = mods()
-    from activemodelbplus.integrator import Integrator, Model, Stencil
     K, dt = 50, 1e-3
     phi, delta, params, models = L.generate_pairs(48, 128, K, [2000, 6000, 12000], seed=11)
     tr = (phi[:, :40], delta[:, :40], params[:40])
@@ -312,24 +310,66 @@ def test_training_gains_over_untrained_and_naive_coarse_step():
     before = L.evaluate(net, *te, K=K, dt=dt)
     L.train(net, *tr, K=K, dt=dt, iters=400, batch=8, lr=2e-3)
     after = L.evaluate(net, *te, K=K, dt=dt)
-    # naive: one Euler step with dt' = K dt from the same states (deterministic)
-    num = den = 0.0
-    for s in range(phi.shape[0]):
-        for i in range(40, 48):
-            m = models[i]
-            quiet = Model(m.a, m.b, m.c, m.kappa, m.lamb, m.zeta, 0.0)
-            sim = Integrator(phi[s, i].cpu().numpy(), Stencil(K * dt, 1, 1), quiet, precision="f64")
-            try:
-                sim.run(1)
-                pred = sim.field - phi[s, i].cpu().numpy()
-            except Exception:
-                pred = np.full(phi.shape[2:], np.inf)
-            d = delta[s, i].cpu().numpy().astype(np.float64)
-            num += float(np.square(pred - d).sum())
-            den += float(np.square(d).sum())
-    naive = num / den
     assert after < 0.5 * before, (before, after)
-    assert after < naive, (after, naive)
+
+
+def _rollout_stats(net, field, stencil, model, t_end, seeds):
+    """Mean S(k) mean wavenumber and droplet count of learned rollouts (no residual checks:
+    every macro step is the network's) over noise seeds."""
+    from activemodelbplus import learned as L
+    from activemodelbplus.analysis import count_droplets, mean_wavenumber, structure_factor
+    ks, ds = [], []
+    for sd in seeds:
+        st = L.LearnedStepper(net, field, stencil, model, K=50, seed=sd, check_every=10 ** 6, tol=1e9)
+        st.run_for_time(t_end)
+        f = st.field  # fixed point: always finite (a diverging rollout saturates at the bound)
+        k, S, _ = structure_factor(f, phi0=float(field.mean()))
+        ks.append(mean_wavenumber(k, S))
+        ds.append(count_droplets(f, float(field.mean())))
+    return float(np.mean(ks)), float(np.mean(ds))
+
+
+def test_trained_rollout_beats_the_linear_part_alone():
+    """The method without the network is the exact linear K-step propagator alone (the
+    network's flux set to zero). Rolled out to t = 200 on 256^2 AMB+ (zeta=-4, lambda=-1,
+    T=0.05) without residual checks, the shipped network's end states match the plain FP32
+    integrator's S(k) mean wavenumber and droplet count far more closely than the
+    linear-part-only macro steps do."""
+    import os
+    torch, L, N = mods()
+    from activemodelbplus.analysis import count_droplets, mean_wavenumber, structure_factor
+    from activemodelbplus.integrator import Integrator, Model, Stencil
+    here = os.path.dirname(L.__file__)
+    net = L.FluxNet.load(os.path.join(here, "weights", "fluxnet_k50.npz"))
+    zero = L.FluxNet.load(os.path.join(here, "weights", "fluxnet_k50.npz"))
+    for w in zero.weights[-1:]:
+        w.zero_()
+    for b in zero.biases[-1:]:
+        b.zero_()
+    zero.refresh()
+    field = -0.4 + 0.01 * np.random.default_rng(5).standard_normal((256, 256))
+    stencil, model = Stencil(1e-3, 1, 1), Model(-0.25, 0, 0.25, 1, -1, -4, 0.05)
+    t_end = 200.0
+    pk, pd = [], []
+    for sd in (1, 2):
+        sim = Integrator(field, stencil, model, precision="f32", seed=sd)
+        sim.run(int(round(t_end / stencil.dt)))
+        f = sim.field
+        k, S, _ = structure_factor(f, phi0=float(field.mean()))
+        pk.append(mean_wavenumber(k, S))
+        pd.append(count_droplets(f, float(field.mean())))
+    plain_k, plain_d = float(np.mean(pk)), float(np.mean(pd))
+    net_k, net_d = _rollout_stats(net, field, stencil, model, t_end, (0, 1))
+    lin_k, lin_d = _rollout_stats(zero, field, stencil, model, t_end, (0, 1))
+    err_net = abs(net_k - plain_k) / plain_k
+    err_lin = abs(lin_k - plain_k) / plain_k
+    derr_net = abs(net_d - plain_d) / plain_d
+    derr_lin = abs(lin_d - plain_d) / plain_d
+    print(f"k_avg plain {plain_k:.4f} net {net_k:.4f} linear-only {lin_k:.4f}; "
+          f"droplets plain {plain_d:.1f} net {net_d:.1f} linear-only {lin_d:.1f}")
+    assert err_net < 0.05, err_net
+    assert derr_net < 0.15, derr_net
+    assert err_lin > 3 * err_net or derr_lin > 3 * derr_net, (err_net, err_lin, derr_net, derr_lin)
 
 
 def test_filtered_macro_noise_matches_k_plain_steps():
