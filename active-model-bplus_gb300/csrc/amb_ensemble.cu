@@ -4,9 +4,10 @@
 // are captured once into a CUDA graph and replayed, and the step index lives in
 // device memory so the same graph serves every chunk.
 //
-// Task table: each replica is cut into 112-column strips and row segments; the
-// segment height is chosen for the whole ensemble from the device's resident
-// warp-pair count (waves x (rows + pipeline fill) minimised), larger tasks first.
+// Task table: each replica is cut into 112-column strips and row segments, larger
+// tasks first. The segment height is chosen per size class (replicas of one shape) by
+// measurement at creation, starting from the occupancy model's choice for the whole
+// ensemble (waves x (rows + pipeline fill) minimised).
 // The reference has no counterpart: it runs one integrator per process.
 #include "amb_gb300.h"
 #include "amb_kernels.h"
@@ -29,6 +30,12 @@ struct amb_ensemble
     void* d_coefs = nullptr;
     amb::EnsembleTask* d_tasks = nullptr;
     int ntasks = 0, seg_h = 0;
+    struct SizeClass
+    {
+        int ny, nx, seg_h;  // shape and the segment height of its tasks
+    };
+    std::vector<SizeClass> classes;
+    std::vector<int> class_of;  // replica -> size class
     int64_t* d_step = nullptr;
     int64_t step = 0;
     int* d_flag = nullptr;
@@ -81,6 +88,100 @@ namespace
         return amb::launch_sliding_ensemble(h->d_reps, h->d_coefs, h->d_tasks, h->ntasks, parity, h->d_step, offset,
                                             h->precision == AMB_F32C ? amb::COMP_BF16 : amb::COMP_NONE,
                                             h->noise ? amb::NOISE_PHILOX : amb::NOISE_OFF, h->stream);
+    }
+
+    // Tasks of every replica (112-column strips x row segments of its class's height), the
+    // tallest first.
+    std::vector<amb::EnsembleTask> make_tasks(const amb_ensemble* h)
+    {
+        std::vector<amb::EnsembleTask> tasks;
+        for (int r = 0; r < h->nrep; ++r)
+        {
+            const int h_r = std::min(h->classes[h->class_of[r]].seg_h, h->ny[r]);
+            const int strips = (h->nx[r] + 111) / 112;
+            for (int r0 = 0; r0 < h->ny[r]; r0 += h_r)
+                for (int sidx = 0; sidx < strips; ++sidx)
+                    tasks.push_back({r, sidx, r0, std::min(r0 + h_r, h->ny[r])});
+        }
+        std::stable_sort(tasks.begin(), tasks.end(),
+                         [](const amb::EnsembleTask& a, const amb::EnsembleTask& b) { return a.r1 - a.r0 > b.r1 - b.r0; });
+        return tasks;
+    }
+
+    // Most tasks any segment height from 16 rows up can give (the table's capacity).
+    size_t max_tasks(const amb_ensemble* h)
+    {
+        size_t n = 0;
+        for (int r = 0; r < h->nrep; ++r) n += size_t((h->nx[r] + 111) / 112) * ((h->ny[r] + 15) / 16);
+        return n;
+    }
+
+    // Segment height per size class by measurement: one pass over the classes (most sites
+    // first), each trying heights of its rows / 1, 2, 3, 4, 6, 8 (at least 16) with the other
+    // classes fixed, timing three whole-ensemble launches per candidate (CUDA events) and keeping
+    // the fastest. The launches read the initial fields (parity 0) and write the spare buffers; the
+    // compensation residuals they touch are zeroed afterwards, so the ensemble starts unchanged.
+    // Every candidate gives bitwise the same fields: only the time differs.
+    cudaError_t tune_segments(amb_ensemble* h)
+    {
+        cudaEvent_t t0, t1;
+        cudaError_t e = cudaEventCreate(&t0);
+        if (e == cudaSuccess) e = cudaEventCreate(&t1);
+        const auto time_table = [&](float* ms) -> cudaError_t {
+            std::vector<amb::EnsembleTask> tasks = make_tasks(h);
+            h->ntasks = int(tasks.size());
+            cudaError_t err = cudaMemcpyAsync(h->d_tasks, tasks.data(), sizeof(amb::EnsembleTask) * tasks.size(),
+                                              cudaMemcpyHostToDevice, h->stream);
+            if (err == cudaSuccess) err = launch_step(h, 0, 0);  // warm-up
+            if (err == cudaSuccess) err = cudaEventRecord(t0, h->stream);
+            for (int i = 0; i < 3 && err == cudaSuccess; ++i) err = launch_step(h, 0, 0);
+            if (err == cudaSuccess) err = cudaEventRecord(t1, h->stream);
+            if (err == cudaSuccess) err = cudaEventSynchronize(t1);
+            if (err == cudaSuccess) err = cudaEventElapsedTime(ms, t0, t1);
+            return err;
+        };
+        std::vector<size_t> order(h->classes.size());
+        for (size_t c = 0; c < order.size(); ++c) order[c] = c;
+        std::vector<double> sites(h->classes.size(), 0.0);
+        for (int r = 0; r < h->nrep; ++r) sites[h->class_of[r]] += double(h->ny[r]) * h->nx[r];
+        std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return sites[a] > sites[b]; });
+        float best_ms = 0.f;
+        if (e == cudaSuccess) e = time_table(&best_ms);
+        for (size_t c : order)
+        {
+            auto& cl = h->classes[c];
+            const int keep = cl.seg_h;
+            int best_h = keep;
+            for (int div : {1, 2, 3, 4, 6, 8})
+            {
+                const int H = std::max(16, (cl.ny + div - 1) / div);
+                if (e != cudaSuccess || H == keep || (div > 1 && H >= cl.ny)) continue;
+                cl.seg_h = H;
+                float ms = 0.f;
+                e = time_table(&ms);
+                if (e == cudaSuccess && ms < best_ms)
+                {
+                    best_ms = ms;
+                    best_h = H;
+                }
+            }
+            cl.seg_h = best_h;
+        }
+        if (e == cudaSuccess)
+        {
+            std::vector<amb::EnsembleTask> tasks = make_tasks(h);
+            h->ntasks = int(tasks.size());
+            e = cudaMemcpyAsync(h->d_tasks, tasks.data(), sizeof(amb::EnsembleTask) * tasks.size(),
+                                cudaMemcpyHostToDevice, h->stream);
+        }
+        for (int r = 0; r < h->nrep && e == cudaSuccess; ++r)
+            if (h->host_reps[r].residual)
+                e = cudaMemsetAsync(h->host_reps[r].residual, 0, size_t(h->ny[r]) * h->nx[r] * sizeof(uint16_t),
+                                    h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+        return e;
     }
 
     // Capture graph_steps (even) steps from the current parity, and the counter advance,
@@ -164,21 +265,20 @@ extern "C" int amb_ensemble_create(int nreplicas, const int* nrows, const int* n
         h->host_reps.push_back(rep);
     }
 
-    // task table
+    // task table: a start from the occupancy model, then segment heights per size class chosen by
+    // measurement (below, once the replicas are on the device)
     int resident = 0;
     if (e == cudaSuccess) e = amb::ensemble_resident_pairs(&resident);
-    std::vector<amb::EnsembleTask> tasks;
     if (e == cudaSuccess)
     {
         double best = 1e300;
         for (int H = 16; H <= 1024; H += 8)
         {
-            long long ntask = 0, rows_max = 0;
+            long long ntask = 0;
             for (int r = 0; r < nreplicas; ++r)
             {
                 int h_r = std::min(H, h->ny[r]);
                 ntask += (long long)((h->nx[r] + 111) / 112) * ((h->ny[r] + h_r - 1) / h_r);
-                rows_max = std::max<long long>(rows_max, h_r);
             }
             long long waves = (ntask + resident - 1) / resident;
             double cost = double(waves) * double(H + 10);
@@ -188,21 +288,24 @@ extern "C" int amb_ensemble_create(int nreplicas, const int* nrows, const int* n
                 h->seg_h = H;
             }
         }
+        // size classes: replicas of one shape share a segment height
         for (int r = 0; r < nreplicas; ++r)
         {
-            int h_r = std::min(h->seg_h, h->ny[r]);
-            int strips = (h->nx[r] + 111) / 112;
-            for (int r0 = 0; r0 < h->ny[r]; r0 += h_r)
-                for (int sidx = 0; sidx < strips; ++sidx)
-                    tasks.push_back({r, sidx, r0, std::min(r0 + h_r, h->ny[r])});
+            size_t c = 0;
+            while (c < h->classes.size() && (h->classes[c].ny != h->ny[r] || h->classes[c].nx != h->nx[r])) ++c;
+            if (c == h->classes.size()) h->classes.push_back({h->ny[r], h->nx[r], std::min(h->seg_h, h->ny[r])});
+            h->class_of.push_back(int(c));
         }
-        std::stable_sort(tasks.begin(), tasks.end(),
-                         [](const amb::EnsembleTask& a, const amb::EnsembleTask& b) { return a.r1 - a.r0 > b.r1 - b.r0; });
+    }
+    std::vector<amb::EnsembleTask> tasks;
+    if (e == cudaSuccess)
+    {
+        tasks = make_tasks(h);
         h->ntasks = int(tasks.size());
     }
     if (e == cudaSuccess) e = dalloc(h, &h->d_reps, sizeof(amb::EnsembleReplica) * nreplicas);
     if (e == cudaSuccess) e = dalloc(h, &h->d_coefs, coefs.size());
-    if (e == cudaSuccess) e = dalloc(h, &h->d_tasks, sizeof(amb::EnsembleTask) * tasks.size());
+    if (e == cudaSuccess) e = dalloc(h, &h->d_tasks, sizeof(amb::EnsembleTask) * max_tasks(h));
     if (e == cudaSuccess) e = dalloc(h, &h->d_step, sizeof(int64_t));
     if (e == cudaSuccess) e = dalloc(h, &h->d_flag, sizeof(int));
     if (e == cudaSuccess)
@@ -212,6 +315,7 @@ extern "C" int amb_ensemble_create(int nreplicas, const int* nrows, const int* n
         e = cudaMemcpy(h->d_tasks, tasks.data(), sizeof(amb::EnsembleTask) * tasks.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(h->d_step, 0, sizeof(int64_t));
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess && h->classes.size() > 0) e = tune_segments(h);
     if (e != cudaSuccess)
     {
         int code = e == cudaErrorMemoryAllocation ? AMB_ERR_NOMEM : AMB_ERR_CUDA;
@@ -280,7 +384,17 @@ extern "C" int amb_ensemble_info(const amb_ensemble* h, int64_t* timestep, int* 
     if (!h) return efail(AMB_ERR_INVALID, "NULL ensemble");
     if (timestep) *timestep = h->step;
     if (ntasks) *ntasks = h->ntasks;
-    if (seg_rows) *seg_rows = h->seg_h;
+    if (seg_rows)  // the segment height of the tallest size class
+    {
+        int tallest = 0;
+        *seg_rows = 0;
+        for (const auto& c : h->classes)
+            if (c.ny > tallest)
+            {
+                tallest = c.ny;
+                *seg_rows = c.seg_h;
+            }
+    }
     return AMB_OK;
 }
 

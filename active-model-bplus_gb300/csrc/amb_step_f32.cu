@@ -685,10 +685,11 @@ namespace amb
         // Batched form: one warp pair per task of a task table that spans many replicas of
         // different sizes and parameters; the step index comes from device memory so that
         // a captured CUDA graph of several steps can be replayed.
-        // (6 one-pair CTAs per SM: at most 168 registers without spills; the per-replica
-        // coefficients come from a table in global memory, not from kernel parameters)
+        // The per-replica coefficients are copied from their table into the pair's shared memory
+        // at the start of the task and read from there (8 one-pair CTAs per SM, as the
+        // single-field kernel: at most 128 registers).
         template <int COMP, int NOISE>
-        __global__ void __launch_bounds__(64, 6)
+        __global__ void __launch_bounds__(64, 8)
         sliding_ensemble_kernel(const EnsembleReplica* __restrict__ reps, const Coef* __restrict__ coefs,
                                 const EnsembleTask* __restrict__ tasks, int parity,
                                 const int64_t* __restrict__ step_counter, int step_offset)
@@ -700,7 +701,14 @@ namespace amb
             const EnsembleReplica& rd = reps[bt.replica];
             StepParams p = rd.p;
             p.step = *step_counter + step_offset;
-            const Coef& k = coefs[bt.replica];
+            Coef* kc = reinterpret_cast<Coef*>(smem_raw + sizeof(PairSmem));
+            {
+                const uint32_t* src = reinterpret_cast<const uint32_t*>(coefs + bt.replica);
+                uint32_t* dst = reinterpret_cast<uint32_t*>(kc);
+                for (int i = threadIdx.x; i < int(sizeof(Coef) / 4); i += 64) dst[i] = src[i];
+            }
+            __syncthreads();
+            const Coef& k = *kc;
             Task t;
             int c0 = bt.strip * kOut;
             t.store_lo = c0;
@@ -818,6 +826,12 @@ namespace amb
 {
     size_t sliding_coef_bytes() { return sizeof(sliding::Coef); }
 
+    namespace
+    {
+        // A pair's shared memory plus its replica's coefficient block.
+        constexpr size_t ensemble_smem_bytes() { return sizeof(sliding::PairSmem) + sizeof(sliding::Coef); }
+    }
+
     void sliding_make_coef(const StepParams& p, void* out)
     {
         sliding::Coef k(p);
@@ -842,12 +856,12 @@ namespace amb
             if (!configured)
             {
                 cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     int(sizeof(PairSmem)));
+                                                     int(ensemble_smem_bytes()));
                 if (e != cudaSuccess) return e;
                 configured = true;
             }
-            kern<<<ntasks, 64, sizeof(PairSmem), stream>>>(reps, static_cast<const Coef*>(coefs), tasks, parity,
-                                                          step_counter, step_offset);
+            kern<<<ntasks, 64, ensemble_smem_bytes(), stream>>>(reps, static_cast<const Coef*>(coefs), tasks, parity,
+                                                               step_counter, step_offset);
             return cudaGetLastError();
         }
     }
@@ -856,11 +870,12 @@ namespace amb
     {
         using namespace sliding;
         auto kern = sliding_ensemble_kernel<COMP_BF16, NOISE_PHILOX>;
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(PairSmem)));
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(ensemble_smem_bytes()));
         int dev = 0, sms = 0, blocks = 0;
         if (e == cudaSuccess) e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, 64, sizeof(PairSmem));
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, 64, ensemble_smem_bytes());
         if (e == cudaSuccess) *out = blocks * sms > 0 ? blocks * sms : 1;
         return e;
     }

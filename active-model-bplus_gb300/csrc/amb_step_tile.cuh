@@ -71,13 +71,27 @@ namespace amb
         const int ny = p.ny, nx = p.nx;
         const int tid = threadIdx.x, nthr = blockDim.x;
 
-        // Load phi(t) with a 9-site periodic halo.
-        for (int e = tid; e < G::LY * G::LX; e += nthr)
+        // Load phi(t) with a 9-site periodic halo: up to 8 loads per thread issued before any of
+        // them is stored, so their latencies overlap.
+        constexpr int NL = G::LY * G::LX, BATCH = 8;
+        for (int base = tid; base < NL; base += BATCH * nthr)
         {
-            int i = e / G::LX, j = e - i * G::LX;
-            int gr = wrap_index(r0 + i - G::H, ny);
-            int gc = wrap_index(c0 + j - G::H, nx);
-            PHI[e] = load_field<Real, COHERENT>(phi_in + (size_t)gr * nx + gc);
+            Real v[BATCH];
+#pragma unroll
+            for (int u = 0; u < BATCH; ++u)
+            {
+                const int e = base + u * nthr;
+                if (e < NL)
+                {
+                    const int i = e / G::LX, j = e - i * G::LX;
+                    const int gr = wrap_index(r0 + i - G::H, ny);
+                    const int gc = wrap_index(c0 + j - G::H, nx);
+                    v[u] = load_field<Real, COHERENT>(phi_in + (size_t)gr * nx + gc);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < BATCH; ++u)
+                if (base + u * nthr < NL) PHI[base + u * nthr] = v[u];
         }
         __syncthreads();
 

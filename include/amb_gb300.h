@@ -219,7 +219,9 @@ int amb_check_finite_f32(const float* field, int64_t n, int* flag, void* stream)
  * independent replicas — any mix of sizes (ncols >= 112, ncols % 4 == 0) and model
  * parameters, FP32 storage (AMB_F32 or AMB_F32C), one Philox seed each — advanced
  * together: one launch per step covers every replica, and graph_steps (even; 0 = no
- * graph) steps are captured once into a CUDA graph and replayed. */
+ * graph) steps are captured once into a CUDA graph and replayed. Creation times a few
+ * launches to choose the row-segment height of each replica shape (the fields are left as
+ * given). Each replica's result is bitwise that of a single-field run. */
 typedef struct amb_ensemble amb_ensemble;
 int amb_ensemble_create(int nreplicas, const int* nrows, const int* ncols, const double* const* host_fields,
                         const amb_stencil* stencils, const amb_model* models, const uint64_t* seeds, int precision,
@@ -228,6 +230,8 @@ void amb_ensemble_destroy(amb_ensemble* h);
 /* Advance every replica nsteps steps, then check all fields are finite (AMB_ERR_NONFINITE). */
 int amb_ensemble_run(amb_ensemble* h, int nsteps);
 int amb_ensemble_get_field(amb_ensemble* h, int replica, double* host_out);
+/* timestep, warp-pair tasks per step, and the row-segment height of the tallest replicas' tasks
+ * (heights are chosen per replica shape by measurement when the ensemble is created). */
 int amb_ensemble_info(const amb_ensemble* h, int64_t* timestep, int* ntasks, int* seg_rows);
 /* Device-to-device copy of every replica's current field into dst / from src (FP32, packed
  * back to back in replica order, replica r at offset sum_{q<r} nrows_q*ncols_q). Scatter also

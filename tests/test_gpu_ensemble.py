@@ -47,3 +47,28 @@ def test_ensemble_rejects_narrow_replicas_and_nonfinite():
     ens = Ensemble([np.zeros((64, 128)), bad], Stencil(1e-3, 1, 1), Model(-0.25, 0, 0.25, 1, 0, 0, 0))
     with pytest.raises(CudaException):
         ens.run(2)
+
+
+def test_config4_scale_ensemble_replicas_equal_single_runs():
+    """The batched-ensemble configuration at its size: 256 replicas with sizes drawn from
+    {128, 192, 256, 384, 512, 768, 1024}^2 and zeta in [-4, 4], lambda in [-1, 1], phi0 in
+    [-0.6, 0.6], T in [0, 0.1] (a=-0.25, c=0.25, kappa=1, dt=1e-3), FP32-compensated, 12 steps
+    (a 4-step graph replayed three times). The first replica of every size class, and a few more,
+    equal standalone Integrator runs of the same field, parameters and seed bitwise."""
+    from activemodelbplus.integrator import Ensemble, Integrator, Model, Stencil
+    rng = np.random.default_rng(7)
+    sizes = rng.choice([128, 192, 256, 384, 512, 768, 1024], size=256)
+    fields, models = [], []
+    for n in sizes:
+        phi0 = rng.uniform(-0.6, 0.6)
+        fields.append(phi0 + 0.01 * rng.standard_normal((n, n)))
+        models.append(Model(-0.25, 0, 0.25, 1, rng.uniform(-1, 1), rng.uniform(-4, 4), rng.uniform(0, 0.1)))
+    stencil = Stencil(1e-3, 1, 1)
+    ens = Ensemble(fields, stencil, models, precision="f32c", seeds=list(range(256)), graph_steps=4)
+    ens.run(12)
+    picks = sorted({int(np.flatnonzero(sizes == s)[0]) for s in np.unique(sizes)} | {3, 100, 255})
+    for r in picks:
+        sim = Integrator(fields[r], stencil, models[r], precision="f32c", seed=r, kernel="sliding")
+        sim.run(12)
+        assert np.array_equal(ens.field(r), sim.field), (r, sizes[r])
+    ens.close()
