@@ -41,6 +41,7 @@ class amb_kernel_config(ctypes.Structure):
 
 
 AMB_FLAG_PERSISTENT = 1
+AMB_FLAG_FUSED = 2
 
 
 _VP = ctypes.c_void_p

@@ -130,7 +130,7 @@ namespace
         if (cfg.kernel < AMB_KERNEL_AUTO || cfg.kernel > max_kernel) return fail(AMB_ERR_INVALID, "unknown kernel selector");
         if (cfg.seg_rows < 0 || cfg.pairs_per_cta < 0 || cfg.pairs_per_cta > 4 || cfg.pairs_per_cta == 3)
             return fail(AMB_ERR_INVALID, "kernel config: seg_rows >= 0, pairs_per_cta in {0, 1, 2, 4}");
-        if (cfg.flags & ~AMB_FLAG_PERSISTENT) return fail(AMB_ERR_INVALID, "kernel config: unknown flags");
+        if (cfg.flags & ~(AMB_FLAG_PERSISTENT | AMB_FLAG_FUSED)) return fail(AMB_ERR_INVALID, "kernel config: unknown flags");
         return AMB_OK;
     }
 }
@@ -204,7 +204,7 @@ extern "C" int amb_step_f32_ex(const amb_stencil* stencil, const amb_model* mode
         return tile_steps<float>(stencil, model, seed, nrows, ncols, field, spare, res, comp, step0, nsteps,
                                  injected_noise, cfg, as_stream(stream), result_in_spare, "amb_step_f32");
     const int pairs_code = cfg.pairs_per_cta == 1 ? 1 : cfg.pairs_per_cta == 4 ? 3 : cfg.pairs_per_cta == 2 ? 2 : 0;
-    const int variant = (cfg.seg_rows << 4) | pairs_code;
+    const int variant = (cfg.seg_rows << 4) | ((cfg.flags & AMB_FLAG_FUSED) ? 8 : 0) | pairs_code;
     float* cur = field;
     float* nxt = spare;
     for (int s = 0; s < nsteps; ++s)

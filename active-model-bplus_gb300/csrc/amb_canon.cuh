@@ -135,6 +135,21 @@ namespace amb
         return s;
     }
 
+    // mu_p alone at one site (the same operations as canon_stage_a's mu_p).
+    template <typename Real>
+    __device__ __forceinline__ Real canon_mu_p(const Real* u, const Real* m, const Real* d, const Canon<Real>& k)
+    {
+        const Real Am = radd(u[-1], u[1]);
+        const Real A0 = radd(m[-1], m[1]);
+        const Real Ap = radd(d[-1], d[1]);
+        const Real f = m[0];
+        Real l = rmul(k.lA, radd(Am, Ap));
+        l = rfma(k.lB, radd(u[0], d[0]), l);
+        l = rfma(k.lC, A0, l);
+        const Real lap = rfma(k.lD, f, l);
+        return rfma(k.nkappa, lap, rmul(rfma(rfma(k.c, f, k.b), f, k.a), f));
+    }
+
     // sum_j c_j (g[+j] - g[-j]), j = 1..4, in that order (first a product, then fused).
     template <typename Real>
     __device__ __forceinline__ Real canon_d8(const Real (&c)[4], Real m1, Real p1, Real m2, Real p2, Real m3, Real p3,

@@ -65,6 +65,17 @@ namespace amb
             int abort;                   // set by the producer when a row never arrived
         };
 
+        // Shared memory of one warp that runs every stage of its strip (the fused form).
+        struct __align__(16) WarpSmem
+        {
+            float phi[kRing][kRowF];     // phi row ring (TMA destination)
+            float mup[kMupRing][kCols];  // mu_p rows k-9..k (D8_y reads k-8..k-1, J1_x reads k-8)
+            float j1y[kJ1Ring][kCols];   // J1_y rows k-12..k-4
+            float xch[kCols];            // J1_x row exchange
+            float dtj[kDelay][kCols];    // divTj delay ring
+            uint64_t bar[kRing];         // one mbarrier per phi ring slot
+        };
+
         __device__ __forceinline__ uint32_t smem_u32(const void* p)
         {
             return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -120,7 +131,8 @@ namespace amb
         };
 
         // Lane 0 fetches local row m (global row r0 - 9 + m) of the strip window into ring slot m % 16.
-        __device__ __forceinline__ void issue_row(PairSmem& sm, const float* __restrict__ phi, int ny, int nx,
+        template <typename Smem>
+        __device__ __forceinline__ void issue_row(Smem& sm, const float* __restrict__ phi, int ny, int nx,
                                                   const Task& t, int m)
         {
             int slot = m & (kRing - 1);
@@ -661,6 +673,370 @@ namespace amb
             }
         }
 
+        // One warp runs every stage of its strip: the producer's and the consumer's work of each
+        // round in one instruction stream, with no hand-off buffers and no barrier between warps
+        // (the only synchronisation is the warp's own, around the J1_x row exchange). The same
+        // operations in the same order as the warp pair, so the same bits.
+        template <int COMP, int NOISE>
+        __device__ __forceinline__ void fused_strip(WarpSmem& sm, const float* __restrict__ phi_in,
+                                                    float* __restrict__ phi_out, __nv_bfloat16* residual,
+                                                    const StepParams& p, const Coef& k,
+                                                    const float* __restrict__ injected, const Task& t, int lane)
+        {
+            const int ny = p.ny, nx = p.nx;
+            const int H = t.r1 - t.r0;
+            const int nrows = H + 18;   // local rows 0 .. H+17 (global r0-9 .. r1+8)
+            const int total = H + 16;   // rounds kl = 1 .. H+16
+            const int gcol = wrap_index(t.c0 - 8 + 4 * lane, nx);
+            const int scol = t.c0 - 8 + 4 * lane;
+            const bool out_lane = lane >= 2 && lane < 30 && scol >= t.store_lo && scol < nx;
+            const int own = 4 + 4 * lane;
+
+            if (lane == 0)
+            {
+                for (int s = 0; s < kRing; ++s) mbar_init(&sm.bar[s], 1);
+                asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+                for (int m = 0; m <= kLead && m < nrows; ++m) issue_row(sm, phi_in, ny, nx, t, m);
+            }
+            __syncwarp();
+            int issued = min(kLead, nrows - 1);
+            bool ok = mbar_wait(&sm.bar[0], 0);
+            ok &= mbar_wait(&sm.bar[1], 0);
+            bool failed = !__all_sync(0xffffffffu, ok);
+            int waited = failed ? -1 : 1;
+
+            float fm[6], fz[6];
+#pragma unroll
+            for (int q = 0; q < 6; ++q)
+            {
+                fm[q] = sm.phi[0][own - 1 + q];
+                fz[q] = sm.phi[1][own - 1 + q];
+            }
+            float xin[4] = {0.f, 0.f, 0.f, 0.f};  // xi_y of this round's J1_y row, formed one round ahead
+            int nrow = 0;
+            int ms = 1;      // mu_p ring slot of row kl  (kl mod 10)
+            int js = 5;      // J1_y ring slot of row kl-4 ((kl - 4) mod 9), from round 9 on
+            float sxm[3][4], dxm[3][4], sxj[3][4], dxj[3][4];
+            float jcy[4], jcx[4];  // J_c of row kl-1
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) sxm[i][q] = dxm[i][q] = sxj[i][q] = dxj[i][q] = 0.f;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) jcy[q] = jcx[q] = 0.f;
+            int grow = t.r0;   // output row of the next output round
+            int mo = 9;        // mu_p ring slot of the output row ((kl - 8) mod 10)
+            float xnx[4] = {0.f, 0.f, 0.f, 0.f};
+            uint2 rnext = make_uint2(0u, 0u);
+
+            const auto round = [&](int kl, auto j1_tag, auto dy_tag) {
+                constexpr bool J1 = decltype(j1_tag)::value, OUT = decltype(dy_tag)::value;
+                const int mnew = kl + 1;
+                if (!failed)
+                {
+                    bool okw = mbar_wait(&sm.bar[mnew & (kRing - 1)], (mnew >> 4) & 1);
+                    if (__all_sync(0xffffffffu, okw)) waited = mnew;
+                    else failed = true;
+                }
+                // ---- stage A at local row kl
+                float lap[4], gx[4], gy[4], f0[4];
+                {
+                    const float* rp = sm.phi[mnew & (kRing - 1)];
+                    float4 vp = lds4(rp + own);
+                    float pL = __shfl_up_sync(0xffffffffu, vp.w, 1);
+                    float pR = __shfl_down_sync(0xffffffffu, vp.x, 1);
+                    if (lane == 0) pL = rp[own - 1];
+                    if (lane == 31) pR = rp[own + 4];
+                    float fp[6] = {pL, vp.x, vp.y, vp.z, vp.w, pR};
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                    {
+                        float Am = fm[q] + fm[q + 2], Dm = fm[q + 2] - fm[q];
+                        float A0 = fz[q] + fz[q + 2], D0 = fz[q + 2] - fz[q];
+                        float Ap = fp[q] + fp[q + 2], Dp = fp[q + 2] - fp[q];
+                        float f = fz[q + 1];
+                        float l = k.lA * (Am + Ap);
+                        l = fmaf(k.lB, fm[q + 1] + fp[q + 1], l);
+                        l = fmaf(k.lC, A0, l);
+                        lap[q] = fmaf(k.lD, f, l);
+                        gx[q] = fmaf(k.gxb, D0, k.gxa * (Dm + Dp));
+                        gy[q] = fmaf(k.gyb, fp[q + 1] - fm[q + 1], k.gya * (Ap - Am));
+                        f0[q] = f;
+                    }
+#pragma unroll
+                    for (int q = 0; q < 6; ++q)
+                    {
+                        fm[q] = fz[q];
+                        fz[q] = fp[q];
+                    }
+                }
+                float mup[4], mua[4], ncy[4], ncx[4];
+#pragma unroll
+                for (int h2 = 0; h2 < 2; ++h2)
+                {
+                    const int q = 2 * h2;
+                    const float2 f = make_float2(f0[q], f0[q + 1]), l2 = make_float2(lap[q], lap[q + 1]);
+                    const float2 x2 = make_float2(gx[q], gx[q + 1]), y2 = make_float2(gy[q], gy[q + 1]);
+                    const float2 poly = __fmul2_rn(__ffma2_rn(__ffma2_rn(k.cp, f, k.bp), f, k.ap), f);
+                    const float2 mp = __ffma2_rn(k.nkappap, l2, poly);
+                    const float2 ma = __fmul2_rn(k.lambdap, __ffma2_rn(y2, y2, __fmul2_rn(x2, x2)));
+                    const float2 zl = __fmul2_rn(k.zetap, l2);
+                    const float2 cy = __fmul2_rn(zl, y2), cx = __fmul2_rn(zl, x2);
+                    mup[q] = mp.x; mup[q + 1] = mp.y;
+                    mua[q] = ma.x; mua[q + 1] = ma.y;
+                    ncy[q] = cy.x; ncy[q + 1] = cy.y;
+                    ncx[q] = cx.x; ncx[q + 1] = cx.y;
+                }
+                sts4(&sm.mup[ms][4 * lane], mup);
+                float dy8[4] = {0.f, 0.f, 0.f, 0.f};
+                if constexpr (J1)
+                {
+                    // ---- J1_y at local row kl-4 from mu_p rows kl-8..kl (own columns)
+                    const int bm = ms + 2 < kMupRing ? ms + 2 : ms + 2 - kMupRing;
+                    const float* mb = &sm.mup[bm][4 * lane];
+                    float4 m[9];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i)
+                        if (i != 4) m[i] = lds4(ring_row<kMupRing>(mb, bm, i));
+                    m[4] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    m[8] = make_float4(mup[0], mup[1], mup[2], mup[3]);
+                    const float2 xlo = make_float2(xin[0], xin[1]), xhi = make_float2(xin[2], xin[3]);
+                    normals<NOISE>(p, k, injected, nrow, gcol, 0, xin);
+                    nrow = nrow + 1 == ny ? 0 : nrow + 1;
+                    float2 slo, shi;
+                    d8y_pairs(m, k.ny8p, slo, shi);
+                    slo = __ffma2_rn(k.magp, xlo, slo);
+                    shi = __ffma2_rn(k.magp, xhi, shi);
+                    const float j1y[4] = {slo.x, slo.y, shi.x, shi.y};
+                    sts4(&sm.j1y[js][4 * lane], j1y);
+                    if constexpr (OUT)
+                    {
+                        // ---- DY8 at local row kl-8 from J1_y rows kl-12..kl-4
+                        const int bj = js + 1 < kJ1Ring ? js + 1 : js + 1 - kJ1Ring;
+                        const float* jb = &sm.j1y[bj][4 * lane];
+                        float4 j[9];
+#pragma unroll
+                        for (int i = 0; i < 8; ++i)
+                            if (i != 4) j[i] = lds4(ring_row<kJ1Ring>(jb, bj, i));
+                        j[4] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        j[8] = make_float4(j1y[0], j1y[1], j1y[2], j1y[3]);
+                        float2 dlo, dhi;
+                        d8y_pairs(j, k.py8p, dlo, dhi);
+                        dy8[0] = dlo.x; dy8[1] = dlo.y; dy8[2] = dhi.x; dy8[3] = dhi.y;
+                    }
+                    js = js + 1 == kJ1Ring ? 0 : js + 1;
+                }
+                // ---- Tjhung chain: J2 at row kl-1, divTj at row kl-2
+                {
+                    float mL = __shfl_up_sync(0xffffffffu, mua[3], 1);
+                    float mR = __shfl_down_sync(0xffffffffu, mua[0], 1);
+                    float mm[6] = {mL, mua[0], mua[1], mua[2], mua[3], mR};
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                    {
+                        sxm[0][q] = sxm[1][q]; sxm[1][q] = sxm[2][q];
+                        dxm[0][q] = dxm[1][q]; dxm[1][q] = dxm[2][q];
+                        sxm[2][q] = fmaf(0.1f, mm[q] + mm[q + 2], 0.3f * mm[q + 1]);
+                        dxm[2][q] = mm[q + 2] - mm[q];
+                    }
+                    float j2y[4], j2x[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q += 2)
+                    {
+                        const auto P = [q](const float (&v)[4]) { return make_float2(v[q], v[q + 1]); };
+                        const float2 vy = __ffma2_rn(k.ndyp, sub2(P(sxm[2]), P(sxm[0])), P(jcy));
+                        const float2 vx = __ffma2_rn(k.jx3p, P(dxm[1]),
+                                                     __ffma2_rn(k.jx1p, __fadd2_rn(P(dxm[2]), P(dxm[0])), P(jcx)));
+                        j2y[q] = vy.x; j2y[q + 1] = vy.y;
+                        j2x[q] = vx.x; j2x[q + 1] = vx.y;
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                    {
+                        jcy[q] = ncy[q];  // J_c at row kl, for the next round
+                        jcx[q] = ncx[q];
+                    }
+                    float yL = __shfl_up_sync(0xffffffffu, j2y[3], 1);
+                    float yR = __shfl_down_sync(0xffffffffu, j2y[0], 1);
+                    float xL = __shfl_up_sync(0xffffffffu, j2x[3], 1);
+                    float xR = __shfl_down_sync(0xffffffffu, j2x[0], 1);
+                    float yy[6] = {yL, j2y[0], j2y[1], j2y[2], j2y[3], yR};
+                    float xx[6] = {xL, j2x[0], j2x[1], j2x[2], j2x[3], xR};
+                    float dtj[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                    {
+                        sxj[0][q] = sxj[1][q]; sxj[1][q] = sxj[2][q];
+                        dxj[0][q] = dxj[1][q]; dxj[1][q] = dxj[2][q];
+                        sxj[2][q] = fmaf(0.1f, yy[q] + yy[q + 2], 0.3f * yy[q + 1]);
+                        dxj[2][q] = xx[q + 2] - xx[q];
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; q += 2)
+                    {
+                        const auto P = [q](const float (&v)[4]) { return make_float2(v[q], v[q + 1]); };
+                        float2 v = __fmul2_rn(k.tx1p, __fadd2_rn(P(dxj[0]), P(dxj[2])));
+                        v = __ffma2_rn(k.tx3p, P(dxj[1]), v);
+                        v = __ffma2_rn(k.dyInvp, sub2(P(sxj[2]), P(sxj[0])), v);
+                        dtj[q] = v.x; dtj[q + 1] = v.y;
+                    }
+                    sts4(&sm.dtj[(kl - 2) & (kDelay - 1)][4 * lane], dtj);
+                }
+                if constexpr (OUT)
+                {
+                    // ---- output local row kl-8 (global row grow)
+                    const int lo = kl - 8;
+                    const float* mrow = sm.mup[mo];
+                    mo = mo + 1 == kMupRing ? 0 : mo + 1;
+                    __syncwarp();  // the mu_p row's neighbour columns were written by other lanes
+                    float4 ml = lds4(&mrow[(4 * lane - 4) & (kCols - 1)]);
+                    float4 mc = lds4(&mrow[4 * lane]);
+                    float4 mr = lds4(&mrow[(4 * lane + 4) & (kCols - 1)]);
+                    float mu[12] = {ml.x, ml.y, ml.z, ml.w, mc.x, mc.y, mc.z, mc.w, mr.x, mr.y, mr.z, mr.w};
+                    float xi[4] = {xnx[0], xnx[1], xnx[2], xnx[3]};
+                    const int gnext = grow + 1 == ny ? 0 : grow + 1;
+                    normals<NOISE>(p, k, injected, gnext, gcol, 1, xnx);
+                    uint2 rv = rnext;
+                    if constexpr (COMP == COMP_BF16)
+                        rnext = *reinterpret_cast<const uint2*>(residual + (size_t)gnext * nx + gcol);
+                    float j1x[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                    {
+                        float s = k.nx8[0] * (mu[q + 5] - mu[q + 3]);
+                        s = fmaf(k.nx8[1], mu[q + 6] - mu[q + 2], s);
+                        s = fmaf(k.nx8[2], mu[q + 7] - mu[q + 1], s);
+                        s = fmaf(k.nx8[3], mu[q + 8] - mu[q], s);
+                        j1x[q] = fmaf(k.mag, xi[q], s);
+                    }
+                    sts4(&sm.xch[4 * lane], j1x);
+                    __syncwarp();
+                    float4 jl = lds4(&sm.xch[(4 * lane - 4) & (kCols - 1)]);
+                    float4 jr = lds4(&sm.xch[(4 * lane + 4) & (kCols - 1)]);
+                    float jj[12] = {jl.x, jl.y, jl.z, jl.w, j1x[0], j1x[1], j1x[2], j1x[3], jr.x, jr.y, jr.z, jr.w};
+                    __syncwarp();
+                    float4 dt4 = lds4(&sm.dtj[lo & (kDelay - 1)][4 * lane]);
+                    const float dtv[4] = {dt4.x, dt4.y, dt4.z, dt4.w};
+                    float4 ph4 = lds4(&sm.phi[lo & (kRing - 1)][own]);
+                    float fo[4] = {ph4.x, ph4.y, ph4.z, ph4.w};
+                    const size_t gi = (size_t)grow * nx + gcol;
+                    grow = gnext;
+                    float rr[4] = {0.f, 0.f, 0.f, 0.f};
+                    if constexpr (COMP == COMP_BF16)
+                    {
+                        rr[0] = __uint_as_float(rv.x << 16);
+                        rr[1] = __uint_as_float(rv.x & 0xffff0000u);
+                        rr[2] = __uint_as_float(rv.y << 16);
+                        rr[3] = __uint_as_float(rv.y & 0xffff0000u);
+                    }
+                    float dx8[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                    {
+                        float d = k.px8[0] * (jj[q + 5] - jj[q + 3]);
+                        d = fmaf(k.px8[1], jj[q + 6] - jj[q + 2], d);
+                        d = fmaf(k.px8[2], jj[q + 7] - jj[q + 1], d);
+                        dx8[q] = fmaf(k.px8[3], jj[q + 8] - jj[q], d);
+                    }
+                    float nf[4], nr[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q += 2)
+                    {
+                        const auto P = [q](const float (&v)[4]) { return make_float2(v[q], v[q + 1]); };
+                        const float2 div = __fadd2_rn(P(dx8), __fadd2_rn(P(dtv), P(dy8)));
+                        float2 vf, vr;
+                        if constexpr (COMP == COMP_BF16)
+                        {
+                            const float2 F = __ffma2_rn(k.dtp, div, P(rr));
+                            vf = sub2(P(fo), F);
+                            vr = __fadd2_rn(sub2(vf, P(fo)), F);
+                        }
+                        else
+                        {
+                            vf = __ffma2_rn(k.ndtp, div, P(fo));
+                            vr = make_float2(0.f, 0.f);
+                        }
+                        nf[q] = vf.x; nf[q + 1] = vf.y;
+                        nr[q] = vr.x; nr[q + 1] = vr.y;
+                    }
+                    if (failed) nf[0] = nf[1] = nf[2] = nf[3] = __int_as_float(0x7fc00000);
+                    if (out_lane)
+                    {
+                        *reinterpret_cast<float4*>(phi_out + gi) = make_float4(nf[0], nf[1], nf[2], nf[3]);
+                        if constexpr (COMP == COMP_BF16)
+                        {
+                            __nv_bfloat162 lo2 = __floats2bfloat162_rn(nr[0], nr[1]);
+                            __nv_bfloat162 hi2 = __floats2bfloat162_rn(nr[2], nr[3]);
+                            uint2 w;
+                            w.x = *reinterpret_cast<uint32_t*>(&lo2);
+                            w.y = *reinterpret_cast<uint32_t*>(&hi2);
+                            *reinterpret_cast<uint2*>(residual + gi) = w;
+                        }
+                    }
+                }
+                ms = ms + 1 == kMupRing ? 0 : ms + 1;
+                // ---- refill: this warp read local row kl-10 last in round kl-2; fetch row kl+6 into its slot
+                __syncwarp();
+                if (lane == 0 && !failed && kl + 6 < nrows)
+                {
+                    fence_proxy_async();
+                    issue_row(sm, phi_in, ny, nx, t, kl + 6);
+                }
+                if (!failed && kl + 6 < nrows) issued = kl + 6;
+            };
+            using F = std::false_type;
+            using T = std::true_type;
+            for (int base = 0; base < 6; base += 3)
+            {
+#pragma unroll
+                for (int ph = 1; ph <= 3; ++ph) round(base + ph, F{}, F{});  // rounds 1..6
+            }
+            round(7, F{}, F{});
+            round(8, F{}, F{});
+            // J1_y rows from local row 5 (round 9) on: xi_y of that row (global r0 - 4) now
+            nrow = wrap_index(t.r0 - 4, ny);
+            normals<NOISE>(p, k, injected, nrow, gcol, 0, xin);
+            nrow = nrow + 1 == ny ? 0 : nrow + 1;
+            for (int base = 8; base < 14; base += 3)
+            {
+#pragma unroll
+                for (int ph = 1; ph <= 3; ++ph) round(base + ph, T{}, F{});  // rounds 9..14
+            }
+            round(15, T{}, F{});
+            round(16, T{}, F{});
+            // output rounds: xi_x and residual of the first output row (global r0)
+            normals<NOISE>(p, k, injected, grow, gcol, 1, xnx);
+            if constexpr (COMP == COMP_BF16)
+                rnext = *reinterpret_cast<const uint2*>(residual + (size_t)grow * nx + gcol);
+            for (int base = 16; base < total; base += 3)
+            {
+#pragma unroll
+                for (int ph = 1; ph <= 3; ++ph)
+                {
+                    const int kl = base + ph;
+                    if (kl > total) break;
+                    round(kl, T{}, T{});
+                }
+            }
+            if (failed)  // drain this warp's copies in flight (bounded) before the CTA can exit
+                for (int m = waited + 1; m <= issued; ++m) mbar_wait(&sm.bar[m & (kRing - 1)], (m >> 4) & 1);
+        }
+
+        template <int COMP, int NOISE, int WARPS>
+        __global__ void __launch_bounds__(32 * WARPS)
+        sliding_fused_kernel(const float* __restrict__ phi_in, float* __restrict__ phi_out, __nv_bfloat16* residual,
+                             const StepParams p, const Coef k, const float* __restrict__ injected, int seg_h,
+                             int nstrips, int ntasks)
+        {
+            extern __shared__ __align__(16) unsigned char smem_raw[];
+            const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            const int task = blockIdx.x * WARPS + warp;
+            if (task >= ntasks) return;
+            WarpSmem& sm = reinterpret_cast<WarpSmem*>(smem_raw)[warp];
+            const Task t = make_task(task, nstrips, seg_h, p.ny, p.nx);
+            fused_strip<COMP, NOISE>(sm, phi_in, phi_out, residual, p, k, injected, t, lane);
+        }
+
         template <int COMP, int NOISE, int PAIRS>
         __global__ void __launch_bounds__(64 * PAIRS)
         sliding_kernel(const float* __restrict__ phi_in, float* __restrict__ phi_out, __nv_bfloat16* residual,
@@ -783,6 +1159,47 @@ namespace amb
             return cudaGetLastError();
         }
 
+        template <int COMP, int NOISE, int WARPS>
+        cudaError_t launch_fused(const float* phi_in, float* phi_out, __nv_bfloat16* comp, const StepParams& p,
+                                 const float* injected, int seg_h, cudaStream_t stream)
+        {
+            using namespace sliding;
+            const size_t smem = sizeof(WarpSmem) * WARPS;
+            auto kern = sliding_fused_kernel<COMP, NOISE, WARPS>;
+            static int resident = 0;  // per kernel variant; the process drives one device type
+            if (resident == 0)
+            {
+                cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+                if (e != cudaSuccess) return e;
+                int dev = 0, sms = 0, blocks = 0;
+                if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+                if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+                if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, 32 * WARPS, smem)) != cudaSuccess)
+                    return e;
+                resident = blocks * WARPS * sms > 0 ? blocks * WARPS * sms : WARPS;
+            }
+            if (seg_h <= 0) seg_h = choose_seg_h(p.ny, p.nx, resident);
+            const int nstrips = (p.nx + kOut - 1) / kOut;
+            const int nsegs = (p.ny + seg_h - 1) / seg_h;
+            const int ntasks = nstrips * nsegs;
+            const Coef k(p);
+            kern<<<(ntasks + WARPS - 1) / WARPS, 32 * WARPS, smem, stream>>>(phi_in, phi_out, comp, p, k, injected,
+                                                                            seg_h, nstrips, ntasks);
+            return cudaGetLastError();
+        }
+
+        template <int COMP, int WARPS>
+        cudaError_t by_noise_fused(const float* phi_in, float* phi_out, __nv_bfloat16* comp, const StepParams& p,
+                                   int noise_mode, const float* injected, int seg_h, cudaStream_t stream)
+        {
+            switch (noise_mode)
+            {
+            case NOISE_PHILOX: return launch_fused<COMP, NOISE_PHILOX, WARPS>(phi_in, phi_out, comp, p, injected, seg_h, stream);
+            case NOISE_INJECTED: return launch_fused<COMP, NOISE_INJECTED, WARPS>(phi_in, phi_out, comp, p, injected, seg_h, stream);
+            default: return launch_fused<COMP, NOISE_OFF, WARPS>(phi_in, phi_out, comp, p, injected, seg_h, stream);
+            }
+        }
+
         template <int COMP, int WPB>
         cudaError_t by_noise(const float* phi_in, float* phi_out, __nv_bfloat16* comp, const StepParams& p,
                              int noise_mode, const float* injected, int seg_h, cudaStream_t stream)
@@ -801,14 +1218,27 @@ namespace amb
         return choose_seg_h(ny, nx, 152 * 8);
     }
 
-    // variant: 0 = defaults; otherwise (seg_h << 4) | code with code 1 -> 1, 2 -> 2, 3 -> 4 warp pairs per CTA.
+    // variant: 0 = defaults; otherwise (seg_h << 4) | fused (8) | code, code 1 -> 1, 2 -> 2, 3 -> 4 warp
+    // pairs (fused: warps) per CTA.
     cudaError_t launch_step_f32_sliding(const float* phi_in, float* phi_out, __nv_bfloat16* comp, int comp_mode,
                                         const StepParams& p, int noise_mode, const float* injected, int variant,
                                         cudaStream_t stream)
     {
         if (!step_f32_sliding_supported(p.ny, p.nx, variant)) return cudaErrorNotSupported;
         int seg_h = variant >> 4;
-        int wpb = variant & 15;
+        int wpb = variant & 7;
+        if (variant & 8)
+        {
+            if (comp_mode == COMP_BF16)
+            {
+                if (wpb == 1) return by_noise_fused<COMP_BF16, 1>(phi_in, phi_out, comp, p, noise_mode, injected, seg_h, stream);
+                if (wpb == 2) return by_noise_fused<COMP_BF16, 2>(phi_in, phi_out, comp, p, noise_mode, injected, seg_h, stream);
+                return by_noise_fused<COMP_BF16, 4>(phi_in, phi_out, comp, p, noise_mode, injected, seg_h, stream);
+            }
+            if (wpb == 1) return by_noise_fused<COMP_NONE, 1>(phi_in, phi_out, comp, p, noise_mode, injected, seg_h, stream);
+            if (wpb == 2) return by_noise_fused<COMP_NONE, 2>(phi_in, phi_out, comp, p, noise_mode, injected, seg_h, stream);
+            return by_noise_fused<COMP_NONE, 4>(phi_in, phi_out, comp, p, noise_mode, injected, seg_h, stream);
+        }
         if (wpb == 0) wpb = 1;
         if (comp_mode == COMP_BF16)
         {

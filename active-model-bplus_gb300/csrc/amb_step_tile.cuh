@@ -104,9 +104,13 @@ namespace amb
             bool in_a = i >= -2 && i < TY + 2 && j >= -2 && j < TX + 2;
             if (!in_plus && !in_a) continue;
             const Real* m = PHI + (i + G::H) * G::LX + (j + G::H);
+            if (!in_a)  // the arms of the plus need mu_p only
+            {
+                MUP[e] = canon_mu_p(m - G::LX, m, m + G::LX, k);
+                continue;
+            }
             const SiteA<Real> s = canon_stage_a(m - G::LX, m, m + G::LX, k);
             MUP[e] = s.mup;
-            if (in_a)
             {
                 MUA[(i + 2) * G::AX + (j + 2)] = s.mua;
                 if (i >= -1 && i < TY + 1 && j >= -1 && j < TX + 1)

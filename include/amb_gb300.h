@@ -87,7 +87,9 @@ typedef struct amb_model
  * flags: AMB_FLAG_PERSISTENT (tile kernel): all nsteps of the call in one cooperative launch,
  *   a grid-wide barrier between the steps (for grids too small to fill the GPU, where a launch
  *   per step costs more than the step; ignored while the stream is being captured). The
- *   results are bitwise those of one launch per step. */
+ *   results are bitwise those of one launch per step.
+ *   AMB_FLAG_FUSED (sliding kernel): one warp per strip runs every stage (no producer/consumer
+ *   warp pair); pairs_per_cta then counts warps per CTA (1, 2 or 4). Bitwise the same results. */
 typedef struct amb_kernel_config
 {
     int kernel;
@@ -96,6 +98,7 @@ typedef struct amb_kernel_config
     int flags;
 } amb_kernel_config;
 #define AMB_FLAG_PERSISTENT 1
+#define AMB_FLAG_FUSED 2
 
 /* Number of FP64 planes written by amb_terms_*: mu_p, mu_a, J_p(y,x), J_l(y,x), J_c(y,x), J_r(y,x). */
 #define AMB_NTERMS 10

@@ -228,3 +228,31 @@ def test_tile_persistent_injected_noise_and_fp64():
         assert rc == 0, N.last_error()
         outs.append((b if flag.value else a).cpu().numpy())
     assert np.array_equal(outs[0], outs[1])
+
+
+# ------------------------------------------------- the fused (one warp per strip) form
+
+@pytest.mark.parametrize("shape", [(256, 256), (200, 140), (37, 340), (17, 256), (96, 448), (5, 136), (40, 112),
+                                   (64, 116)])
+@pytest.mark.parametrize("T", [0.0, 0.05])
+def test_fused_is_bitwise_the_warp_pair(shape, T):
+    """One warp per strip running every stage (AMB_FLAG_FUSED) gives the warp pair's results
+    bit for bit, plain and compensated, for 1, 2 and 4 warps per CTA."""
+    field = initial(shape, seed=shape[0] + 3)
+    p = Params(T=T, **AMB)
+    for comp in (False, True):
+        ref = run_f32(field, p, 21, kernel=2, comp=comp)
+        for warps in (1, 2, 4):
+            got = run_f32(field, p, 21, kernel=2, comp=comp, pairs=warps, flags=2)
+            assert np.array_equal(ref, got), (comp, warps, np.abs(ref - got).max())
+
+
+def test_fused_injected_noise_and_segments():
+    rng = np.random.default_rng(19)
+    field = initial((144, 560), seed=19)
+    noise = rng.standard_normal((6, 2, 144, 560))
+    p = Params(T=0.05, **AMB)
+    ref = run_f32(field, p, 6, kernel=2, comp=True, injected=noise)
+    for seg in (1, 16, 37, 100):
+        got = run_f32(field, p, 6, kernel=2, comp=True, injected=noise, seg_rows=seg, pairs=2, flags=2)
+        assert np.array_equal(ref, got), seg
