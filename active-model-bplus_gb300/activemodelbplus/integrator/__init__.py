@@ -183,7 +183,8 @@ class Integrator:
             bitwise equal fields (the same arithmetic at every site), so the choice
             changes the time, never the result.
         launch: explicit launch shape: for kernel="sliding" (FP32 storage) {"seg_rows": h,
-            "pairs_per_cta": p}; for kernel="tile" {"pairs_per_cta": g (256-thread groups per CTA),
+            "pairs_per_cta": p, "fused": bool (one warp per strip runs every stage; p then counts
+            warps)}; for kernel="tile" {"pairs_per_cta": g (256-thread groups per CTA),
             "persistent": bool (all steps of a run() in one launch)}; e.g. a configuration the
             autotuner reported.
     """
@@ -229,7 +230,8 @@ class Integrator:
         if launch is not None:
             if kernel not in ("sliding", "tile") or (precision == "f64" and kernel != "tile"):
                 raise ValueError('launch= applies to kernel="sliding" (FP32 storage) or kernel="tile"')
-            flags = N.AMB_FLAG_PERSISTENT if launch.get("persistent", False) else 0
+            flags = ((N.AMB_FLAG_PERSISTENT if launch.get("persistent", False) else 0)
+                     | (N.AMB_FLAG_FUSED if launch.get("fused", False) else 0))
             self._launch_cfg = N.amb_kernel_config(_KERNELS[kernel], int(launch.get("seg_rows", 0)),
                                                    int(launch.get("pairs_per_cta", 0)), flags)
         self._tuned = None
@@ -241,7 +243,8 @@ class Integrator:
             names = {N.AMB_KERNEL_TILE: "tile", N.AMB_KERNEL_SLIDING: "sliding"}
             self._tuned = {"kernel": names.get(cfg.kernel, "auto"), "seg_rows": cfg.seg_rows,
                            "pairs_per_cta": cfg.pairs_per_cta,
-                           "persistent": bool(cfg.flags & N.AMB_FLAG_PERSISTENT), "us_per_step": us.value}
+                           "persistent": bool(cfg.flags & N.AMB_FLAG_PERSISTENT),
+                           "fused": bool(cfg.flags & N.AMB_FLAG_FUSED), "us_per_step": us.value}
         del lib
 
     # -------------------------------------------------------------- plumbing

@@ -3,8 +3,9 @@
 //
 // Candidates: the tile kernel with 256, 512 or 1024 threads per CTA, launched once per step
 // or once for all steps (persistent, grid barrier between steps), and the warp-pair sliding
-// kernel with 1, 2 or 4 pairs per CTA and row-segment heights from 2 rows up to the whole
-// grid (plus the occupancy model's own choice). All candidates give bitwise the same field. Each is timed with CUDA events over a few steps on
+// kernel with 1, 2 or 4 pairs per CTA (or, fused, 1, 2 or 4 single warps per CTA) and row-segment
+// heights from 2 rows up to the whole grid (plus the occupancy model's own choice). All candidates
+// give bitwise the same field. Each is timed with CUDA events over a few steps on
 // scratch buffers of the same shape; the fastest few are timed again and the best
 // is kept in a process-wide cache keyed by (device, nrows, ncols, compensated,
 // noise), which AMB_KERNEL_AUTO consults. The kernels do the same work whatever the
@@ -104,11 +105,12 @@ extern "C" int amb_autotune_f32(const amb_stencil* stencil, const amb_model* mod
         for (int flags : {0, AMB_FLAG_PERSISTENT}) cands.push_back({AMB_KERNEL_TILE, 0, groups, flags});
     if (ncols >= 112 && ncols % 4 == 0)
         for (int pairs : {1, 2, 4})
-        {
-            cands.push_back({AMB_KERNEL_SLIDING, 0, pairs, 0});
-            for (int seg = 2; seg < 2 * nrows && seg <= 4096; seg *= 2)
-                cands.push_back({AMB_KERNEL_SLIDING, std::min(seg, nrows), pairs, 0});
-        }
+            for (int flags : {0, AMB_FLAG_FUSED})
+            {
+                cands.push_back({AMB_KERNEL_SLIDING, 0, pairs, flags});
+                for (int seg = 2; seg < 2 * nrows && seg <= 4096; seg *= 2)
+                    cands.push_back({AMB_KERNEL_SLIDING, std::min(seg, nrows), pairs, flags});
+            }
 
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);

@@ -278,6 +278,31 @@ def test_stepper_conserves_and_falls_back():
     assert abs(m1 - m0) < 64 * 128  # plain FP32 spans conserve to rounding
 
 
+def test_drift_inside_a_long_span_is_rolled_back():
+    """The residual check is a spot check of each span's last macro step, and a span is kept or
+    redone as a whole. Here the shipped network runs until the adaptive interval has grown to its
+    longest (8 macro steps); then its flux is corrupted. The next span's end check fails, the
+    whole span is redone by the plain integrator (none of its learned steps survives), and the
+    interval returns to the shortest."""
+    import os
+    torch, L, N = mods()
+    from activemodelbplus.integrator import Model, Stencil
+    here = os.path.dirname(L.__file__)
+    net = L.FluxNet.load(os.path.join(here, "weights", "fluxnet_k50.npz"))
+    field = -0.4 + 0.01 * np.random.default_rng(9).standard_normal((128, 256))
+    st = L.LearnedStepper(net, field, Stencil(1e-3, 1, 1), Model(-0.25, 0, 0.25, 1, -1, -4, 0.05), K=50,
+                          check_every=2, max_check_every=8, tol=1.0, residual_sigma=2.0, use_graph=False)
+    st.advance(2 + 4 + 8)  # accepted spans of 2, 4 and 8 macro steps: the interval is now 8
+    assert st.fallback_spans == 0 and st.learned_steps == 14 and st.interval == 8
+    learned_before, state = st.learned_steps, st.phi_q.clone()
+    net.weights[-1].mul_(50.0)  # the flux drifts far off from here on
+    net.refresh()
+    st.advance(8)
+    assert st.fallback_spans == 1 and st.learned_steps == learned_before  # the span was redone
+    assert st.interval == 2
+    assert not torch.equal(st.phi_q, state) and np.isfinite(st.field).all()
+
+
 def test_linear_macro_step_matches_the_propagator():
     """With a zero network flux and T = 0, a learned macro step is the linear part alone: the
     field becomes irfft2(a(k)^K phi_hat) up to the fixed-point rounding (2^-24 per face)."""
