@@ -101,7 +101,9 @@ namespace
     {
         const size_t n = size_t(nrows) * ncols;
         const int mode = noise_mode_for(model, injected_noise);
-        const int groups = cfg.pairs_per_cta == 0 ? 1 : cfg.pairs_per_cta;
+        // default CTA width: 512 threads (measured fastest for FP64 at 1024^2-4096^2 and for FP32
+        // small grids; the FP32 autotuner names its own)
+        const int groups = cfg.pairs_per_cta == 0 ? 2 : cfg.pairs_per_cta;
         if ((cfg.flags & AMB_FLAG_PERSISTENT) && nsteps > 1 && !capturing(stream))
         {
             amb::StepParams p = make_params(stencil, model, seed, nrows, ncols, step0);

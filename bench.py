@@ -182,15 +182,32 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def measured_traffic(args):
-    """Per-launch DRAM bytes of the step kernel from the committed ncu summary, if any."""
+def _profile_record():
     path = os.path.join(ROOT, "profiles", "step_kernel_traffic.json")
     if not os.path.exists(path):
-        return None
+        return {}
     with open(path) as f:
-        d = json.load(f)
-    key = f"{args.precision}_{args.size}"
-    return d.get(key)
+        return json.load(f)
+
+
+def measured_traffic(args):
+    """Per-launch DRAM bytes of the step kernel from the committed ncu summary, if any."""
+    return _profile_record().get(f"{args.precision}_{args.size}")
+
+
+def issue_roofline(args, value: float, sm_mhz):
+    """The step kernel's own binding limit: issue slots. With S thread-instruction slots per
+    output site (ncu: smsp__inst_executed x 32 / sites, committed with the profile), the GPU can
+    issue at most SMs x 4 schedulers x 32 lanes x clock / S site-updates per second; frac is the
+    measured rate against that limit."""
+    slots = _profile_record().get(f"{args.precision}_{args.size}_slots_per_site")
+    if not slots:
+        return None
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = float(sm_mhz) if sm_mhz else 2070.0
+    limit = sms * 4 * 32 * mhz * 1e6 / slots / 1e9
+    return {"slots_per_site": slots, "sm_mhz": mhz, "limit_gsites": limit, "frac": value / limit}
 
 
 def _timed_sample(run, sites: int, seconds: float):
@@ -256,6 +273,24 @@ def cpu_baseline(w, seconds: float = 10.0):
         return port
     out["port"] = port
     return out
+
+
+def fp64_path(w, stencil, model, field, nsteps: int = 20):
+    """The FP64 path (the parity path, 1e-12 against the reference) on the same workload: nsteps
+    in one Integrator.run, CUDA events, after 3 untimed steps."""
+    import torch
+    from activemodelbplus.integrator import Integrator
+    sim = Integrator(field, stencil, model, precision="f64", seed=1)
+    sim.run(3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    sim._launch(nsteps)
+    e1.record()
+    e1.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    sites = w["ny"] * w["nx"]
+    return {"value": nsteps * sites / sec / 1e9, "unit": UNIT, "dtype": "f64",
+            "sample": f"{nsteps} steps of the {w['ny']}x{w['nx']} workload, tile kernel (512-thread CTAs), CUDA events"}
 
 
 def reference_gpu_baseline(w, nsteps: int = 20):
@@ -433,9 +468,12 @@ def run_ours(args, w, rank, world, dist):
         "gpu_launches": args.steps * (args.inner + 1),
         "clocks": clocks.summary(),
     }
+    csum = line["clocks"] or {}
+    line["roofline"]["issue"] = issue_roofline(args, value, csum.get("sm_mhz"))
     if not args.no_cpu and world == 1:
         line["cpu_baseline"] = cpu_baseline(w)
         line["reference_gpu"] = reference_gpu_baseline(w)
+        line["fp64"] = fp64_path(w, stencil, model, field)
     if not args.no_learned and world == 1 and os.path.exists(args.weights):
         # the metric's second half: learned surrogate vs plain FP32 time to t = 10^3 at 512^2
         # (one noise seed per arm here; `bench.py --learned` runs ten per arm)
