@@ -725,6 +725,19 @@ class Ensemble:
     def seeds(self):
         return list(self._seeds)
 
+    @property
+    def fused(self) -> bool:
+        """Whether the step kernel runs one warp per task doing every stage (True) or a
+        producer/consumer warp pair (False); creation picks the faster by measurement, and
+        assigning sets it. Both give bitwise the same fields."""
+        form = ctypes.c_int()
+        _check(N.lib().amb_ensemble_form(self._h, -1, ctypes.byref(form)))
+        return bool(form.value)
+
+    @fused.setter
+    def fused(self, value: bool) -> None:
+        _check(N.lib().amb_ensemble_form(self._h, 1 if value else 0, None))
+
     def __len__(self):
         return len(self._shapes)
 

@@ -89,6 +89,7 @@ SIGNATURES = {
     "amb_ensemble_run": (_I, [_VP, _I]),
     "amb_ensemble_get_field": (_I, [_VP, _I, _VP]),
     "amb_ensemble_info": (_I, [_VP, ctypes.POINTER(_I64), _IP, _IP]),
+    "amb_ensemble_form": (_I, [_VP, _I, _IP]),
     "amb_radial_spectrum": (_I, [_VP, _I, _I, ctypes.c_double, ctypes.c_double, _VP, _I, _VP, _VP, _VP]),
     "amb_label_components_f64": (_I, [_VP, _I, _I, ctypes.c_double, _VP, _VP, _VP]),
     "amb_label_components_f32": (_I, [_VP, _I, _I, ctypes.c_double, _VP, _VP, _VP]),

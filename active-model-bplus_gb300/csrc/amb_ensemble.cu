@@ -30,6 +30,7 @@ struct amb_ensemble
     void* d_coefs = nullptr;
     amb::EnsembleTask* d_tasks = nullptr;
     int ntasks = 0, seg_h = 0;
+    bool fused = false;  // one warp per task (fused form) instead of a warp pair; chosen by measurement
     struct SizeClass
     {
         int ny, nx, seg_h;  // shape and the segment height of its tasks
@@ -87,7 +88,7 @@ namespace
     {
         return amb::launch_sliding_ensemble(h->d_reps, h->d_coefs, h->d_tasks, h->ntasks, parity, h->d_step, offset,
                                             h->precision == AMB_F32C ? amb::COMP_BF16 : amb::COMP_NONE,
-                                            h->noise ? amb::NOISE_PHILOX : amb::NOISE_OFF, h->stream);
+                                            h->noise ? amb::NOISE_PHILOX : amb::NOISE_OFF, h->fused, h->stream);
     }
 
     // Tasks of every replica (112-column strips x row segments of its class's height), the
@@ -119,7 +120,8 @@ namespace
     // Segment height per size class by measurement: one pass over the classes (most sites
     // first), each trying heights of its rows / 1, 2, 3, 4, 6, 8 (at least 16) with the other
     // classes fixed, timing three whole-ensemble launches per candidate (CUDA events) and keeping
-    // the fastest. The launches read the initial fields (parity 0) and write the spare buffers; the
+    // the fastest; one such pass with the warp-pair kernel and one with the fused single-warp
+    // kernel, and the faster of the two is kept. The launches read the initial fields (parity 0) and write the spare buffers; the
     // compensation residuals they touch are zeroed afterwards, so the ensemble starts unchanged.
     // Every candidate gives bitwise the same fields: only the time differs.
     cudaError_t tune_segments(amb_ensemble* h)
@@ -145,27 +147,42 @@ namespace
         std::vector<double> sites(h->classes.size(), 0.0);
         for (int r = 0; r < h->nrep; ++r) sites[h->class_of[r]] += double(h->ny[r]) * h->nx[r];
         std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return sites[a] > sites[b]; });
-        float best_ms = 0.f;
-        if (e == cudaSuccess) e = time_table(&best_ms);
-        for (size_t c : order)
-        {
-            auto& cl = h->classes[c];
-            const int keep = cl.seg_h;
-            int best_h = keep;
-            for (int div : {1, 2, 3, 4, 6, 8})
+        // one coordinate-descent pass per form (warp pair, fused single warp); the faster form wins
+        const auto pass = [&](float* best_ms) {
+            if (e == cudaSuccess) e = time_table(best_ms);
+            for (size_t c : order)
             {
-                const int H = std::max(16, (cl.ny + div - 1) / div);
-                if (e != cudaSuccess || H == keep || (div > 1 && H >= cl.ny)) continue;
-                cl.seg_h = H;
-                float ms = 0.f;
-                e = time_table(&ms);
-                if (e == cudaSuccess && ms < best_ms)
+                auto& cl = h->classes[c];
+                const int keep = cl.seg_h;
+                int best_h = keep;
+                for (int div : {1, 2, 3, 4, 6, 8})
                 {
-                    best_ms = ms;
-                    best_h = H;
+                    const int H = std::max(16, (cl.ny + div - 1) / div);
+                    if (e != cudaSuccess || H == keep || (div > 1 && H >= cl.ny)) continue;
+                    cl.seg_h = H;
+                    float ms = 0.f;
+                    e = time_table(&ms);
+                    if (e == cudaSuccess && ms < *best_ms)
+                    {
+                        *best_ms = ms;
+                        best_h = H;
+                    }
                 }
+                cl.seg_h = best_h;
             }
-            cl.seg_h = best_h;
+        };
+        const std::vector<amb_ensemble::SizeClass> start = h->classes;
+        float pair_ms = 0.f, fused_ms = 0.f;
+        h->fused = false;
+        pass(&pair_ms);
+        const std::vector<amb_ensemble::SizeClass> pair_classes = h->classes;
+        h->classes = start;
+        h->fused = true;
+        pass(&fused_ms);
+        if (e == cudaSuccess && pair_ms <= fused_ms)
+        {
+            h->fused = false;
+            h->classes = pair_classes;
         }
         if (e == cudaSuccess)
         {
@@ -268,7 +285,7 @@ extern "C" int amb_ensemble_create(int nreplicas, const int* nrows, const int* n
     // task table: a start from the occupancy model, then segment heights per size class chosen by
     // measurement (below, once the replicas are on the device)
     int resident = 0;
-    if (e == cudaSuccess) e = amb::ensemble_resident_pairs(&resident);
+    if (e == cudaSuccess) e = amb::ensemble_resident_pairs(&resident, false);
     if (e == cudaSuccess)
     {
         double best = 1e300;
@@ -376,6 +393,25 @@ extern "C" int amb_ensemble_get_field(amb_ensemble* h, int replica, double* host
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return ecuda(e, "amb_ensemble_get_field");
     for (size_t i = 0; i < n; ++i) host_out[i] = double(tmp[i]);
+    return AMB_OK;
+}
+
+extern "C" int amb_ensemble_form(amb_ensemble* h, int set, int* form)
+{
+    if (!h || set < -1 || set > 1) return efail(AMB_ERR_INVALID, "amb_ensemble_form: bad arguments");
+    if (set >= 0 && (set == 1) != h->fused)
+    {
+        cudaError_t e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) return ecuda(e, "amb_ensemble_form");
+        for (auto& g : h->graph)  // captured with the other kernel
+            if (g)
+            {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+        h->fused = set == 1;
+    }
+    if (form) *form = h->fused ? 1 : 0;
     return AMB_OK;
 }
 

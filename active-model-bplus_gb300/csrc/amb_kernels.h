@@ -48,10 +48,11 @@ namespace amb
     size_t sliding_coef_bytes();
     void sliding_make_coef(const StepParams& p, void* out);  // host: per-replica coefficient block
     int sliding_default_seg_h_for(int ny, int nx, int resident_pairs);
+    // fused: one warp per task running every stage (otherwise a producer/consumer warp pair).
     cudaError_t launch_sliding_ensemble(const EnsembleReplica* reps, const void* coefs, const EnsembleTask* tasks,
                                         int ntasks, int parity, const int64_t* step_counter, int step_offset,
-                                        int comp_mode, int noise_mode, cudaStream_t stream);
-    cudaError_t ensemble_resident_pairs(int* out);
+                                        int comp_mode, int noise_mode, bool fused, cudaStream_t stream);
+    cudaError_t ensemble_resident_pairs(int* out, bool fused);
 
     template <typename Real>
     cudaError_t launch_terms(const Real* phi, double* out, const StepParams& p, int noise_mode, const Real* injected,

@@ -1097,6 +1097,39 @@ namespace amb
             else
                 consumer<COMP, NOISE>(sm, rd.phi[parity ^ 1], rd.residual, p, k, nullptr, t, lane, 1);
         }
+
+        // The batched form with one warp per task running every stage (the fused form), its
+        // replica's coefficient block in shared memory beside the warp's rings.
+        template <int COMP, int NOISE>
+        __global__ void __launch_bounds__(32)
+        sliding_ensemble_fused_kernel(const EnsembleReplica* __restrict__ reps, const Coef* __restrict__ coefs,
+                                      const EnsembleTask* __restrict__ tasks, int parity,
+                                      const int64_t* __restrict__ step_counter, int step_offset)
+        {
+            extern __shared__ __align__(16) unsigned char smem_raw[];
+            const int lane = threadIdx.x & 31;
+            WarpSmem& sm = *reinterpret_cast<WarpSmem*>(smem_raw);
+            const EnsembleTask bt = tasks[blockIdx.x];
+            const EnsembleReplica& rd = reps[bt.replica];
+            StepParams p = rd.p;
+            p.step = *step_counter + step_offset;
+            Coef* kc = reinterpret_cast<Coef*>(smem_raw + sizeof(WarpSmem));
+            {
+                const uint32_t* src = reinterpret_cast<const uint32_t*>(coefs + bt.replica);
+                uint32_t* dst = reinterpret_cast<uint32_t*>(kc);
+                for (int i = lane; i < int(sizeof(Coef) / 4); i += 32) dst[i] = src[i];
+            }
+            __syncwarp();
+            const Coef& k = *kc;
+            Task t;
+            int c0 = bt.strip * kOut;
+            t.store_lo = c0;
+            if (c0 + kOut > p.nx) c0 = p.nx - kOut;
+            t.c0 = c0;
+            t.r0 = bt.r0;
+            t.r1 = bt.r1;
+            fused_strip<COMP, NOISE>(sm, rd.phi[parity], rd.phi[parity ^ 1], rd.residual, p, k, nullptr, t, lane);
+        }
     }
 
     bool step_f32_sliding_supported(int ny, int nx, int variant)
@@ -1258,8 +1291,9 @@ namespace amb
 
     namespace
     {
-        // A pair's shared memory plus its replica's coefficient block.
+        // A pair's (or, fused, a warp's) shared memory plus its replica's coefficient block.
         constexpr size_t ensemble_smem_bytes() { return sizeof(sliding::PairSmem) + sizeof(sliding::Coef); }
+        constexpr size_t ensemble_fused_smem_bytes() { return sizeof(sliding::WarpSmem) + sizeof(sliding::Coef); }
     }
 
     void sliding_make_coef(const StepParams& p, void* out)
@@ -1275,55 +1309,67 @@ namespace amb
 
     namespace
     {
-        template <int COMP, int NOISE>
+        template <int COMP, int NOISE, bool FUSED>
         cudaError_t launch_ensemble_variant(const EnsembleReplica* reps, const void* coefs, const EnsembleTask* tasks,
                                             int ntasks, int parity, const int64_t* step_counter, int step_offset,
                                             cudaStream_t stream)
         {
             using namespace sliding;
-            auto kern = sliding_ensemble_kernel<COMP, NOISE>;
+            auto kern = FUSED ? sliding_ensemble_fused_kernel<COMP, NOISE> : sliding_ensemble_kernel<COMP, NOISE>;
+            const size_t smem = FUSED ? ensemble_fused_smem_bytes() : ensemble_smem_bytes();
             static bool configured = false;
             if (!configured)
             {
-                cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     int(ensemble_smem_bytes()));
+                cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
                 if (e != cudaSuccess) return e;
                 configured = true;
             }
-            kern<<<ntasks, 64, ensemble_smem_bytes(), stream>>>(reps, static_cast<const Coef*>(coefs), tasks, parity,
-                                                               step_counter, step_offset);
+            kern<<<ntasks, FUSED ? 32 : 64, smem, stream>>>(reps, static_cast<const Coef*>(coefs), tasks, parity,
+                                                           step_counter, step_offset);
             return cudaGetLastError();
+        }
+
+        template <bool FUSED>
+        cudaError_t launch_ensemble_form(const EnsembleReplica* reps, const void* coefs, const EnsembleTask* tasks,
+                                         int ntasks, int parity, const int64_t* step_counter, int step_offset,
+                                         int comp_mode, bool noise, cudaStream_t stream)
+        {
+            if (comp_mode == COMP_BF16)
+                return noise ? launch_ensemble_variant<COMP_BF16, NOISE_PHILOX, FUSED>(reps, coefs, tasks, ntasks, parity,
+                                                                                       step_counter, step_offset, stream)
+                             : launch_ensemble_variant<COMP_BF16, NOISE_OFF, FUSED>(reps, coefs, tasks, ntasks, parity,
+                                                                                    step_counter, step_offset, stream);
+            return noise ? launch_ensemble_variant<COMP_NONE, NOISE_PHILOX, FUSED>(reps, coefs, tasks, ntasks, parity,
+                                                                                   step_counter, step_offset, stream)
+                         : launch_ensemble_variant<COMP_NONE, NOISE_OFF, FUSED>(reps, coefs, tasks, ntasks, parity,
+                                                                                step_counter, step_offset, stream);
         }
     }
 
-    cudaError_t ensemble_resident_pairs(int* out)
+    cudaError_t ensemble_resident_pairs(int* out, bool fused)
     {
         using namespace sliding;
-        auto kern = sliding_ensemble_kernel<COMP_BF16, NOISE_PHILOX>;
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             int(ensemble_smem_bytes()));
+        const void* kern = fused ? reinterpret_cast<const void*>(sliding_ensemble_fused_kernel<COMP_BF16, NOISE_PHILOX>)
+                                 : reinterpret_cast<const void*>(sliding_ensemble_kernel<COMP_BF16, NOISE_PHILOX>);
+        const size_t smem = fused ? ensemble_fused_smem_bytes() : ensemble_smem_bytes();
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         int dev = 0, sms = 0, blocks = 0;
         if (e == cudaSuccess) e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, 64, ensemble_smem_bytes());
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, fused ? 32 : 64, smem);
         if (e == cudaSuccess) *out = blocks * sms > 0 ? blocks * sms : 1;
         return e;
     }
 
     cudaError_t launch_sliding_ensemble(const EnsembleReplica* reps, const void* coefs, const EnsembleTask* tasks,
                                         int ntasks, int parity, const int64_t* step_counter, int step_offset,
-                                        int comp_mode, int noise_mode, cudaStream_t stream)
+                                        int comp_mode, int noise_mode, bool fused, cudaStream_t stream)
     {
         if (ntasks <= 0) return cudaSuccess;
         const bool noise = noise_mode == NOISE_PHILOX;
-        if (comp_mode == COMP_BF16)
-            return noise ? launch_ensemble_variant<COMP_BF16, NOISE_PHILOX>(reps, coefs, tasks, ntasks, parity,
-                                                                            step_counter, step_offset, stream)
-                         : launch_ensemble_variant<COMP_BF16, NOISE_OFF>(reps, coefs, tasks, ntasks, parity,
-                                                                         step_counter, step_offset, stream);
-        return noise ? launch_ensemble_variant<COMP_NONE, NOISE_PHILOX>(reps, coefs, tasks, ntasks, parity, step_counter,
-                                                                        step_offset, stream)
-                     : launch_ensemble_variant<COMP_NONE, NOISE_OFF>(reps, coefs, tasks, ntasks, parity, step_counter,
-                                                                     step_offset, stream);
+        return fused ? launch_ensemble_form<true>(reps, coefs, tasks, ntasks, parity, step_counter, step_offset,
+                                                  comp_mode, noise, stream)
+                     : launch_ensemble_form<false>(reps, coefs, tasks, ntasks, parity, step_counter, step_offset,
+                                                   comp_mode, noise, stream);
     }
 }

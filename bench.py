@@ -601,7 +601,8 @@ def run_ensemble(args):
                       "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
                       "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True, "dtype": "f32",
                       "data": "synthetic", "config": {"workload": "ensemble", "replicas": 256, "sites": sites,
-                                                      "inner_steps": args.inner, "tasks": ens.ntasks},
+                                                      "inner_steps": args.inner, "tasks": ens.ntasks,
+                                                      "kernel_form": "fused" if ens.fused else "warp pair"},
                       "clocks": clocks.summary()}), flush=True)
     ens.close()
 

@@ -236,6 +236,11 @@ int amb_ensemble_get_field(amb_ensemble* h, int replica, double* host_out);
 /* timestep, warp-pair tasks per step, and the row-segment height of the tallest replicas' tasks
  * (heights are chosen per replica shape by measurement when the ensemble is created). */
 int amb_ensemble_info(const amb_ensemble* h, int64_t* timestep, int* ntasks, int* seg_rows);
+/* The step kernel's form: 0 = a producer/consumer warp pair per task, 1 = one warp per task
+ * running every stage. Creation chooses the faster by measurement; set = 0 or 1 sets the form,
+ * set = -1 leaves it; *form (may be NULL) receives the form in effect. Both forms give bitwise the
+ * same fields. */
+int amb_ensemble_form(amb_ensemble* h, int set, int* form);
 /* Device-to-device copy of every replica's current field into dst / from src (FP32, packed
  * back to back in replica order, replica r at offset sum_{q<r} nrows_q*ncols_q). Scatter also
  * zeroes the compensation residuals. Synchronous. */

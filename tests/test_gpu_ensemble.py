@@ -23,11 +23,15 @@ def replicas():
 
 
 @pytest.mark.parametrize("precision", ["f32c", "f32"])
-def test_ensemble_replicas_equal_single_runs(precision):
+@pytest.mark.parametrize("fused", [False, True])
+def test_ensemble_replicas_equal_single_runs(precision, fused):
+    """Both kernel forms (warp pair per task, one warp per task)."""
     from activemodelbplus.integrator import Ensemble, Integrator
     fields, stencils, models = replicas()
     seeds = [100 + i for i in range(len(fields))]
     ens = Ensemble(fields, stencils, models, precision=precision, seeds=seeds, graph_steps=8)
+    ens.fused = fused
+    assert ens.fused == fused
     for n in (30, 7, 16):   # 3 graph replays + 6 single steps; 7 single steps (parity flips); 2 replays
         ens.run(n)
     assert ens.timestep == 53
