@@ -682,6 +682,7 @@ class LearnedStepper:
         self.step_dev = torch.zeros(1, dtype=torch.int64, device=dev)
         self.xi = torch.zeros(2, *self.shape, dtype=torch.float32, device=dev)
         self.macro_steps = 0
+        self.extra_steps = 0  # plain Euler steps outside macro steps (run_for_time's remainder)
         self.learned_steps = 0
         self.fallback_spans = 0
         self.residuals = []
@@ -699,7 +700,7 @@ class LearnedStepper:
 
     @property
     def time(self) -> float:
-        return self.macro_steps * self.dtk
+        return self.macro_steps * self.dtk + self.extra_steps * self.stencil.dt
 
     @property
     def field(self) -> np.ndarray:
@@ -779,7 +780,7 @@ class LearnedStepper:
         sim.field_tensor.copy_(self.phi_f)
         if sim._residual is not None:
             sim._residual.zero_()
-        sim._timestep = self.macro_steps * self.K
+        sim._timestep = self.macro_steps * self.K + self.extra_steps
         sim.run(nsteps)
         self._set_from_float(sim.field_tensor)
 
@@ -847,10 +848,17 @@ class LearnedStepper:
         self.net.check_error()
 
     def run_for_time(self, t: float) -> None:
-        n = int(round(t / self.dtk))
-        if not math.isclose(n * self.dtk, t, rel_tol=1e-9, abs_tol=1e-12):
-            raise ValueError(f"t={t} is not a multiple of K dt = {self.dtk}")
+        """Advance by time t (a multiple of dt): as many macro steps of K dt as fit, then the
+        remaining fewer than K Euler steps on the plain integrator."""
+        dt = self.stencil.dt
+        total = int(round(t / dt))
+        if not math.isclose(total * dt, t, rel_tol=1e-9, abs_tol=1e-12):
+            raise ValueError(f"t={t} is not a multiple of dt = {dt}")
+        n, rem = divmod(total, self.K)
         self.advance(n)
+        if rem:
+            self._run_plain(rem)
+            self.extra_steps += rem
 
 
 def next_check_interval(interval: int, residual: float, accepted: bool, tol: float, base: int, longest: int) -> int:
