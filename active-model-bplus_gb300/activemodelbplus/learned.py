@@ -157,22 +157,25 @@ def divergence(flux, dx: float, dy: float):
 # --------------------------------------------------------------- network
 
 class FluxNet:
-    """6 circular 5x5 convolutions (5 -> 32 -> 32 -> 32 -> 32 -> 32 -> 2), GELU between
-    layers, BF16 weights/activations, FP32 accumulation and FP32 master weights."""
+    """``layers`` circular 5x5 convolutions (default 6: 5 -> 32 -> 32 -> 32 -> 32 -> 32 -> 2),
+    GELU between layers, BF16 weights/activations, FP32 accumulation and FP32 master weights."""
 
-    def __init__(self, device=None, seed: int = 0):
+    def __init__(self, device=None, seed: int = 0, layers: int = NLAYERS):
         torch = _torch()
         device = torch.device("cuda") if device is None else torch.device(device)
         g = torch.Generator().manual_seed(int(seed))
+        if int(layers) < 2:
+            raise ValueError("a FluxNet has at least two layers")
         self.device = device
-        self.cin = [CIN0] + [HIDDEN] * 5
-        self.cin_used = [CIN0_USED] + [HIDDEN] * 5
-        self.cout = [HIDDEN] * 5 + [NOUT]
-        self.npad = [HIDDEN] * 5 + [NOUT_PAD]
+        self.nlayers = nl = int(layers)
+        self.cin = [CIN0] + [HIDDEN] * (nl - 1)
+        self.cin_used = [CIN0_USED] + [HIDDEN] * (nl - 1)
+        self.cout = [HIDDEN] * (nl - 1) + [NOUT]
+        self.npad = [HIDDEN] * (nl - 1) + [NOUT_PAD]
         self.weights, self.biases = [], []
-        for l in range(NLAYERS):
+        for l in range(nl):
             fan_in = 25 * self.cin_used[l]
-            std = math.sqrt(2.0 / fan_in) if l < NLAYERS - 1 else 0.1 / math.sqrt(fan_in)
+            std = math.sqrt(2.0 / fan_in) if l < nl - 1 else 0.1 / math.sqrt(fan_in)
             self.weights.append((torch.randn(self.cout[l], self.cin_used[l], 5, 5, generator=g) * std).to(device))
             self.biases.append(torch.zeros(self.npad[l], device=device))
         self.error = torch.zeros(1, dtype=torch.int32, device=device)
@@ -189,11 +192,11 @@ class FluxNet:
         """Rebuild the bf16 operand images after the FP32 weights changed."""
         self._images = [weight_image(w, self.cin[l], self.npad[l]) for l, w in enumerate(self.weights)]
         self._dimages = [None] + [dgrad_image(self.weights[l], self.cin[l], self.npad[l])
-                                  for l in range(1, NLAYERS)]
+                                  for l in range(1, self.nlayers)]
 
     def state_dict(self) -> dict:
         d = {}
-        for l in range(NLAYERS):
+        for l in range(self.nlayers):
             d[f"w{l}"] = self.weights[l].cpu().numpy()
             d[f"b{l}"] = self.biases[l].cpu().numpy()
         d["linear_split"] = np.asarray(int(self.linear_split))
@@ -201,7 +204,7 @@ class FluxNet:
 
     def load_state_dict(self, d) -> None:
         torch = _torch()
-        for l in range(NLAYERS):
+        for l in range(self.nlayers):
             self.weights[l] = torch.as_tensor(np.asarray(d[f"w{l}"]), dtype=torch.float32).to(self.device)
             self.biases[l] = torch.as_tensor(np.asarray(d[f"b{l}"]), dtype=torch.float32).to(self.device)
         self.linear_split = bool(int(np.asarray(d["linear_split"]))) if "linear_split" in d else False
@@ -213,7 +216,8 @@ class FluxNet:
     @classmethod
     def load(cls, path: str, device=None) -> "FluxNet":
         z = np.load(path, allow_pickle=False)
-        net = cls(device=device)
+        layers = sum(1 for k in z.files if k[:1] == "w" and k[1:].isdigit())
+        net = cls(device=device, layers=layers)
         net.load_state_dict({k: z[k] for k in z.files})
         net.K = int(z["K"]) if "K" in z.files else 50
         return net
@@ -227,7 +231,7 @@ class FluxNet:
         B, _, H, W, _ = x.shape
         a = x
         inputs, pres = [], []
-        for l in range(NLAYERS - 1):
+        for l in range(self.nlayers - 1):
             out = torch.empty(B, self.npad[l] // 8, H, W, 8, dtype=torch.bfloat16, device=x.device)
             pre = torch.empty_like(out) if train else None
             conv_forward(a, self._images[l], self.biases[l], cin=self.cin[l], npad=self.npad[l],
@@ -250,9 +254,9 @@ class FluxNet:
         if self._saved is None:
             raise RuntimeError("backward() needs a preceding forward(train=True)")
         inputs, pres = self._saved
-        gw, gb = [None] * NLAYERS, [None] * NLAYERS
+        gw, gb = [None] * self.nlayers, [None] * self.nlayers
         dz = to_chunks(dflux, NOUT_PAD)
-        L = NLAYERS - 1
+        L = self.nlayers - 1
         gw[L] = wgrad_to_weights(conv_wgrad(inputs[L], dz, cin=self.cin[L], npad=self.npad[L], error=self.error),
                                  self.cout[L], self.cin_used[L])
         gb[L] = torch.nn.functional.pad(dflux.sum(dim=(0, 2, 3)), (0, NOUT_PAD - NOUT))
@@ -886,7 +890,7 @@ DEFAULT_SAMPLE_STEPS = (0, 1000, 3000, 10000, 30000, 100000, 200000, 400000, 700
 def train_default(out: str | None = None, *, n_traj: int = 512, size: int = 128, K=50, dt: float = 1e-3,
                   sample_steps=DEFAULT_SAMPLE_STEPS, iters: int = 8000, batch: int = 16, lr: float = 2e-3,
                   seed: int = 0, holdout: float = 0.1, lowpass_sigma: float = 0.0, highpass_weight: float = 1.0,
-                  log=print):
+                  layers: int = NLAYERS, log=print):
     """Generate pairs with the plain integrator, train a FluxNet per K on the device kernels,
     report the held-out errors, and optionally save the weights (``FluxNet.load``; ``out``
     may contain ``{K}``). K may be one step count or a list sharing one set of trajectories.
@@ -906,11 +910,11 @@ def train_default(out: str | None = None, *, n_traj: int = 512, size: int = 128,
         te = (phi[:, -n_test:], delta[:, -n_test:], params[-n_test:])
         # the linear part depends on (a, c, kappa, dt, K, shape) only, which the pair set shares
         lin = LinearPart((size, size), Stencil(dt, 1, 1), Model(a=-0.25, b=0, c=0.25, kappa=1), k)
-        zero = FluxNet(seed=seed)
+        zero = FluxNet(seed=seed, layers=layers)
         for w in zero.weights:
             w.zero_()
         linear_only = evaluate(zero, *te, K=k, dt=dt, linear=lin)
-        net = FluxNet(seed=seed)
+        net = FluxNet(seed=seed, layers=layers)
         before = evaluate(net, *te, K=k, dt=dt, linear=lin)
         t1 = time.perf_counter()
         hist = train(net, *tr, K=k, dt=dt, iters=iters, batch=batch, lr=lr, seed=seed,
@@ -921,14 +925,14 @@ def train_default(out: str | None = None, *, n_traj: int = 512, size: int = 128,
         after = evaluate(net, *te, K=k, dt=dt, linear=lin)
         after_lp = evaluate(net, *te, K=k, dt=dt, lowpass_sigma=2.0, linear=lin)
         net.K = k
-        info = {"n_traj": n_traj, "size": size, "K": k, "dt": dt, "sample_steps": list(sample_steps),
+        info = {"n_traj": n_traj, "size": size, "K": k, "layers": layers, "dt": dt, "sample_steps": list(sample_steps),
                 "iters": iters, "batch": batch, "lr": lr, "seed": seed, "pairs": int(phi.shape[0] * phi.shape[1]),
                 "data_seconds": t_data, "train_seconds": t_train, "heldout_rel_mse_linear_part_only": linear_only,
                 "heldout_rel_mse_untrained": before, "heldout_rel_mse": after,
                 "heldout_rel_mse_lowpass2": after_lp, "lowpass_sigma": lowpass_sigma,
                 "highpass_weight": highpass_weight, "loss_history": hist}
         if log:
-            log(f"K={k}: data {t_data:.1f} s, train {t_train:.1f} s, held-out relative MSE: linear part alone "
+            log(f"K={k}, {layers} layers: data {t_data:.1f} s, train {t_train:.1f} s, held-out relative MSE: linear part alone "
                 f"{linear_only:.3g}, untrained {before:.3g}, trained {after:.3g} (low-passed {after_lp:.3g})")
         if out:
             net.save(out.format(K=k), K=k, dt=dt, heldout_rel_mse=after, heldout_rel_mse_lowpass2=after_lp,
@@ -1075,6 +1079,7 @@ def _main(argv=None) -> int:
     t.add_argument("--sample-steps", default=",".join(str(v) for v in DEFAULT_SAMPLE_STEPS))
     t.add_argument("--lowpass-sigma", type=float, default=0.0)
     t.add_argument("--highpass-weight", type=float, default=1.0)
+    t.add_argument("--layers", type=int, default=NLAYERS, help="convolution layers of the network")
     c = sub.add_parser("compare", help="time to t_end, learned vs plain FP32, from one seeded field")
     c.add_argument("--weights", required=True)
     c.add_argument("--size", type=int, default=512)
@@ -1097,7 +1102,7 @@ def _main(argv=None) -> int:
         Ks = [int(v) for v in a.K.split(",")]
         res = train_default(a.out, n_traj=a.n_traj, size=a.size, iters=a.iters, batch=a.batch, lr=a.lr,
                             seed=a.seed, sample_steps=steps, lowpass_sigma=a.lowpass_sigma,
-                            highpass_weight=a.highpass_weight, K=Ks if len(Ks) > 1 else Ks[0])
+                            highpass_weight=a.highpass_weight, K=Ks if len(Ks) > 1 else Ks[0], layers=a.layers)
         if a.info:
             for k, (_, info) in res.items():
                 with open(a.info.format(K=k), "w") as fh:

@@ -303,6 +303,47 @@ def test_drift_inside_a_long_span_is_rolled_back():
     assert not torch.equal(st.phi_q, state) and np.isfinite(st.field).all()
 
 
+def test_run_for_time_finishes_a_remainder_with_plain_steps():
+    """t = 3 K dt + 7 dt: three macro steps, then seven Euler steps of the plain integrator; the
+    clock reads t, and a t that is not a multiple of dt is refused."""
+    torch, L, N = mods()
+    from activemodelbplus.integrator import Model, Stencil
+    field = -0.4 + 0.01 * np.random.default_rng(4).standard_normal((64, 128))
+    net = L.FluxNet(seed=1)
+    st = L.LearnedStepper(net, field, Stencil(1e-3, 1, 1), Model(-0.25, 0, 0.25, 1, -1, -4, 0.05), K=50,
+                          check_every=10 ** 6, tol=1e9, use_graph=False)
+    st.run_for_time(0.157)
+    assert st.macro_steps == 3 and st.extra_steps == 7
+    assert math.isclose(st.time, 0.157, rel_tol=1e-12)
+    assert np.isfinite(st.field).all()
+    with pytest.raises(ValueError):
+        st.run_for_time(0.0005)
+
+
+def test_learned_end_state_matches_plain_at_t1000():
+    """The shipped K = 50 network against the plain FP32 integrator on the learned-stepper
+    workload (512^2 AMB+, zeta=-4, lambda=-1, T=0.05, phi = -0.4 + 0.01 N(0,1) from numpy seed
+    0, to t = 10^3), ten noise seeds per arm (the comparison `bench.py --learned` reports): the
+    S(k) peak position of the learned mean (sub-bin estimate over the notebook's bins) within
+    2 % of the plain mean, the droplet count within 5 %, the fixed-point mass exact in every
+    run, no fallback span, and the learned runs faster. Both arms are deterministic (fixed
+    Philox keys, fixed-order kernels), so the errors are those of the committed record."""
+    import os
+    torch, L, N = mods()
+    from activemodelbplus.integrator import Model, Stencil
+    here = os.path.dirname(L.__file__)
+    net = L.FluxNet.load(os.path.join(here, "weights", "fluxnet_k50.npz"))
+    field = -0.4 + 0.01 * np.random.default_rng(0).standard_normal((512, 512))
+    res = L.compare_with_plain(net, field, Stencil(1e-3, 1, 1), Model(-0.25, 0, 0.25, 1, -1, -4, 0.05),
+                               t_end=1000.0, seed=0, learned_runs=10)
+    print({k: res[k] for k in ("k_peak_rel_err", "k_peak_rel_err_se", "droplets_rel_err",
+                               "droplets_rel_err_se", "speedup")})
+    assert abs(res["k_peak_rel_err"]) < 0.02, res["k_peak_rel_err"]
+    assert abs(res["droplets_rel_err"]) < 0.05, res["droplets_rel_err"]
+    assert res["learned_mass_q_drift_max"] == 0 and res["learned_fallback_spans"] == 0
+    assert res["speedup"] > 1.0
+
+
 def test_linear_macro_step_matches_the_propagator():
     """With a zero network flux and T = 0, a learned macro step is the linear part alone: the
     field becomes irfft2(a(k)^K phi_hat) up to the fixed-point rounding (2^-24 per face)."""
