@@ -69,7 +69,7 @@ def parse_args(argv=None):
     ap.add_argument("--learned-seeds", type=int, default=10,
                     help="noise seeds per arm of the learned-vs-plain comparison (default line and --learned)")
     ap.add_argument("--no-learned", action="store_true",
-                    help="leave the learned-vs-plain comparison (one seed per arm) out of the default bench line")
+                    help="leave the learned-vs-plain comparison out of the default bench line")
     ap.add_argument("--weights", default=os.path.join(PKG, "activemodelbplus", "weights", "fluxnet_k50.npz"))
     ap.add_argument("--learned-steps", type=int, default=0,
                     help="time N macro steps of the learned stepper on the 512^2 field (after 40 untimed)")
