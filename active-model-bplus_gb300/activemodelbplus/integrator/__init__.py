@@ -185,8 +185,8 @@ class Integrator:
         launch: explicit launch shape: for kernel="sliding" (FP32 storage) {"seg_rows": h,
             "pairs_per_cta": p, "fused": bool (one warp per strip runs every stage; p then counts
             warps)}; for kernel="tile" {"pairs_per_cta": g (256-thread groups per CTA),
-            "persistent": bool (all steps of a run() in one launch)}; e.g. a configuration the
-            autotuner reported.
+            "persistent": bool (all steps of a run() in one launch), "tile_rows": 32 or 28
+            (output tile height)}; e.g. a configuration the autotuner reported.
     """
 
     def __init__(self, field, stencil, model, *, precision: str = "f64", seed: int | None = None,
@@ -230,8 +230,11 @@ class Integrator:
         if launch is not None:
             if kernel not in ("sliding", "tile") or (precision == "f64" and kernel != "tile"):
                 raise ValueError('launch= applies to kernel="sliding" (FP32 storage) or kernel="tile"')
+            if int(launch.get("tile_rows", 32)) not in (28, 32):
+                raise ValueError("tile_rows must be 32 or 28")
             flags = ((N.AMB_FLAG_PERSISTENT if launch.get("persistent", False) else 0)
-                     | (N.AMB_FLAG_FUSED if launch.get("fused", False) else 0))
+                     | (N.AMB_FLAG_FUSED if launch.get("fused", False) else 0)
+                     | (N.AMB_FLAG_TILE_ROWS_28 if int(launch.get("tile_rows", 32)) == 28 else 0))
             self._launch_cfg = N.amb_kernel_config(_KERNELS[kernel], int(launch.get("seg_rows", 0)),
                                                    int(launch.get("pairs_per_cta", 0)), flags)
         self._tuned = None
@@ -244,7 +247,8 @@ class Integrator:
             self._tuned = {"kernel": names.get(cfg.kernel, "auto"), "seg_rows": cfg.seg_rows,
                            "pairs_per_cta": cfg.pairs_per_cta,
                            "persistent": bool(cfg.flags & N.AMB_FLAG_PERSISTENT),
-                           "fused": bool(cfg.flags & N.AMB_FLAG_FUSED), "us_per_step": us.value}
+                           "fused": bool(cfg.flags & N.AMB_FLAG_FUSED),
+                           "tile_rows": 28 if cfg.flags & N.AMB_FLAG_TILE_ROWS_28 else 32, "us_per_step": us.value}
         del lib
 
     # -------------------------------------------------------------- plumbing

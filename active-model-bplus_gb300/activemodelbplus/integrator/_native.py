@@ -42,6 +42,7 @@ class amb_kernel_config(ctypes.Structure):
 
 AMB_FLAG_PERSISTENT = 1
 AMB_FLAG_FUSED = 2
+AMB_FLAG_TILE_ROWS_28 = 4
 
 
 _VP = ctypes.c_void_p

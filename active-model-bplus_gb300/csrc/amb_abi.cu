@@ -104,11 +104,12 @@ namespace
         // default CTA width: 512 threads (measured fastest for FP64 at 1024^2-4096^2 and for FP32
         // small grids; the FP32 autotuner names its own)
         const int groups = cfg.pairs_per_cta == 0 ? 2 : cfg.pairs_per_cta;
+        const bool rows28 = (cfg.flags & AMB_FLAG_TILE_ROWS_28) != 0;
         if ((cfg.flags & AMB_FLAG_PERSISTENT) && nsteps > 1 && !capturing(stream))
         {
             amb::StepParams p = make_params(stencil, model, seed, nrows, ncols, step0);
             cudaError_t e = amb::launch_steps_tile_persistent<Real>(field, spare, res, comp, p, mode, injected_noise,
-                                                                    nsteps, groups, stream);
+                                                                    nsteps, groups, rows28, stream);
             if (e != cudaSuccess) return cuda_fail(e, name);
             if (result_in_spare) *result_in_spare = nsteps & 1;
             return AMB_OK;
@@ -119,7 +120,7 @@ namespace
         {
             amb::StepParams p = make_params(stencil, model, seed, nrows, ncols, step0 + s);
             const Real* inj = injected_noise ? injected_noise + size_t(s) * 2 * n : nullptr;
-            cudaError_t e = amb::launch_step_tile<Real>(cur, nxt, res, comp, p, mode, inj, groups, stream);
+            cudaError_t e = amb::launch_step_tile<Real>(cur, nxt, res, comp, p, mode, inj, groups, rows28, stream);
             if (e != cudaSuccess) return cuda_fail(e, name);
             std::swap(cur, nxt);
         }
@@ -132,7 +133,8 @@ namespace
         if (cfg.kernel < AMB_KERNEL_AUTO || cfg.kernel > max_kernel) return fail(AMB_ERR_INVALID, "unknown kernel selector");
         if (cfg.seg_rows < 0 || cfg.pairs_per_cta < 0 || cfg.pairs_per_cta > 4 || cfg.pairs_per_cta == 3)
             return fail(AMB_ERR_INVALID, "kernel config: seg_rows >= 0, pairs_per_cta in {0, 1, 2, 4}");
-        if (cfg.flags & ~(AMB_FLAG_PERSISTENT | AMB_FLAG_FUSED)) return fail(AMB_ERR_INVALID, "kernel config: unknown flags");
+        if (cfg.flags & ~(AMB_FLAG_PERSISTENT | AMB_FLAG_FUSED | AMB_FLAG_TILE_ROWS_28))
+            return fail(AMB_ERR_INVALID, "kernel config: unknown flags");
         return AMB_OK;
     }
 }

@@ -1,8 +1,9 @@
 // Measured choice of the FP32 step kernel and its launch shape for one grid shape
 // (no reference counterpart; the reference launches fixed 8 x 8 blocks).
 //
-// Candidates: the tile kernel with 256, 512 or 1024 threads per CTA, launched once per step
-// or once for all steps (persistent, grid barrier between steps), and the warp-pair sliding
+// Candidates: the tile kernel with 256, 512 or 1024 threads per CTA, 32 x 32 or 28 x 32 output
+// tiles, launched once per step or once for all steps (persistent, grid barrier between steps),
+// and the warp-pair sliding
 // kernel with 1, 2 or 4 pairs per CTA (or, fused, 1, 2 or 4 single warps per CTA) and row-segment
 // heights from 2 rows up to the whole grid (plus the occupancy model's own choice). All candidates
 // give bitwise the same field. Each is timed with CUDA events over a few steps on
@@ -102,7 +103,8 @@ extern "C" int amb_autotune_f32(const amb_stencil* stencil, const amb_model* mod
 
     std::vector<amb_kernel_config> cands;
     for (int groups : {1, 2, 4})
-        for (int flags : {0, AMB_FLAG_PERSISTENT}) cands.push_back({AMB_KERNEL_TILE, 0, groups, flags});
+        for (int flags : {0, AMB_FLAG_PERSISTENT, AMB_FLAG_TILE_ROWS_28, AMB_FLAG_PERSISTENT | AMB_FLAG_TILE_ROWS_28})
+            cands.push_back({AMB_KERNEL_TILE, 0, groups, flags});
     if (ncols >= 112 && ncols % 4 == 0)
         for (int pairs : {1, 2, 4})
             for (int flags : {0, AMB_FLAG_FUSED})

@@ -12,17 +12,17 @@
 namespace amb
 {
     // Fused single-step tile kernel (amb_step_tile.cuh), one launch = one step; groups x 256
-    // threads per CTA (groups in {1, 2, 4}).
+    // threads per CTA (groups in {1, 2, 4}); 32 x 32 output tiles, or 28 x 32 with rows28.
     template <typename Real>
     cudaError_t launch_step_tile(const Real* phi_in, Real* phi_out, __nv_bfloat16* comp, int comp_mode,
-                                 const StepParams& p, int noise_mode, const Real* injected, int groups,
+                                 const StepParams& p, int noise_mode, const Real* injected, int groups, bool rows28,
                                  cudaStream_t stream);
     // nsteps steps of the tile kernel in one cooperative launch (grid barrier between steps); the
     // result is in a when nsteps is even, in b when odd. injected: nsteps * 2 planes or nullptr.
     template <typename Real>
     cudaError_t launch_steps_tile_persistent(Real* a, Real* b, __nv_bfloat16* comp, int comp_mode,
                                              const StepParams& p, int noise_mode, const Real* injected, int nsteps,
-                                             int groups, cudaStream_t stream);
+                                             int groups, bool rows28, cudaStream_t stream);
 
     // Register-sliding FP32 kernel (amb_step_f32.cu). Returns cudaErrorNotSupported
     // when the grid shape is outside its fast-path constraints.

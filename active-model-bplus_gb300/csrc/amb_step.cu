@@ -7,9 +7,11 @@ namespace amb
 {
     namespace
     {
-        constexpr int TY = 32, TX = 32;
+        // Output tiles of TY rows x 32 columns: 32 x 32, or 28 x 32, which the autotuner picks for
+        // small grids (a 512^2 grid is then 19 x 16 = 304 tiles, two per SM on 152 SMs, against 256
+        // tiles of 32 x 32 that leave 48 SMs with one).
 
-        template <typename Real, int COMP, int NT>
+        template <typename Real, int COMP, int NT, int TY, int TX>
         cudaError_t launch_tile(const Real* phi_in, Real* phi_out, __nv_bfloat16* comp, const StepParams& p,
                                 int noise_mode, const Real* injected, cudaStream_t stream)
         {
@@ -31,7 +33,7 @@ namespace amb
         // All nsteps in one cooperative launch (grid = the resident CTAs, at most one per tile).
         // The grid barrier's arrival counter and error word come from the stream-ordered allocator
         // (cudaMallocAsync), so concurrent launches on other streams never share them.
-        template <typename Real, int COMP, int NT>
+        template <typename Real, int COMP, int NT, int TY, int TX>
         cudaError_t launch_tile_persistent(Real* buf0, Real* buf1, __nv_bfloat16* comp, const StepParams& p,
                                            int noise_mode, const Real* injected, int nsteps, cudaStream_t stream)
         {
@@ -73,64 +75,88 @@ namespace amb
             return e != cudaSuccess ? e : ef;
         }
 
-        template <typename Real, int COMP>
+        template <typename Real, int COMP, int TY>
         cudaError_t by_threads(const Real* phi_in, Real* phi_out, __nv_bfloat16* comp, const StepParams& p,
                                int noise_mode, const Real* injected, int groups, cudaStream_t stream)
         {
-            if (groups == 4) return launch_tile<Real, COMP, 1024>(phi_in, phi_out, comp, p, noise_mode, injected, stream);
-            if (groups == 2) return launch_tile<Real, COMP, 512>(phi_in, phi_out, comp, p, noise_mode, injected, stream);
-            return launch_tile<Real, COMP, 256>(phi_in, phi_out, comp, p, noise_mode, injected, stream);
+            if (groups == 4)
+                return launch_tile<Real, COMP, 1024, TY, 32>(phi_in, phi_out, comp, p, noise_mode, injected, stream);
+            if (groups == 2)
+                return launch_tile<Real, COMP, 512, TY, 32>(phi_in, phi_out, comp, p, noise_mode, injected, stream);
+            return launch_tile<Real, COMP, 256, TY, 32>(phi_in, phi_out, comp, p, noise_mode, injected, stream);
         }
 
-        template <typename Real, int COMP>
+        template <typename Real, int COMP, int TY>
         cudaError_t by_threads_persistent(Real* a, Real* b, __nv_bfloat16* comp, const StepParams& p, int noise_mode,
                                           const Real* injected, int nsteps, int groups, cudaStream_t stream)
         {
             if (groups == 4)
-                return launch_tile_persistent<Real, COMP, 1024>(a, b, comp, p, noise_mode, injected, nsteps, stream);
+                return launch_tile_persistent<Real, COMP, 1024, TY, 32>(a, b, comp, p, noise_mode, injected, nsteps,
+                                                                        stream);
             if (groups == 2)
-                return launch_tile_persistent<Real, COMP, 512>(a, b, comp, p, noise_mode, injected, nsteps, stream);
-            return launch_tile_persistent<Real, COMP, 256>(a, b, comp, p, noise_mode, injected, nsteps, stream);
+                return launch_tile_persistent<Real, COMP, 512, TY, 32>(a, b, comp, p, noise_mode, injected, nsteps,
+                                                                       stream);
+            return launch_tile_persistent<Real, COMP, 256, TY, 32>(a, b, comp, p, noise_mode, injected, nsteps, stream);
+        }
+
+        template <typename Real, int COMP>
+        cudaError_t by_shape(const Real* phi_in, Real* phi_out, __nv_bfloat16* comp, const StepParams& p,
+                             int noise_mode, const Real* injected, int groups, bool rows28, cudaStream_t stream)
+        {
+            if (rows28) return by_threads<Real, COMP, 28>(phi_in, phi_out, comp, p, noise_mode, injected, groups, stream);
+            return by_threads<Real, COMP, 32>(phi_in, phi_out, comp, p, noise_mode, injected, groups, stream);
+        }
+
+        template <typename Real, int COMP>
+        cudaError_t by_shape_persistent(Real* a, Real* b, __nv_bfloat16* comp, const StepParams& p, int noise_mode,
+                                        const Real* injected, int nsteps, int groups, bool rows28, cudaStream_t stream)
+        {
+            if (rows28)
+                return by_threads_persistent<Real, COMP, 28>(a, b, comp, p, noise_mode, injected, nsteps, groups, stream);
+            return by_threads_persistent<Real, COMP, 32>(a, b, comp, p, noise_mode, injected, nsteps, groups, stream);
         }
     }
 
     template <>
     cudaError_t launch_step_tile<double>(const double* phi_in, double* phi_out, __nv_bfloat16* comp, int comp_mode,
                                          const StepParams& p, int noise_mode, const double* injected, int groups,
-                                         cudaStream_t stream)
+                                         bool rows28, cudaStream_t stream)
     {
         (void)comp;
         if (comp_mode != COMP_NONE) return cudaErrorInvalidValue;
-        return by_threads<double, COMP_NONE>(phi_in, phi_out, nullptr, p, noise_mode, injected, groups, stream);
+        return by_shape<double, COMP_NONE>(phi_in, phi_out, nullptr, p, noise_mode, injected, groups, rows28, stream);
     }
 
     template <>
     cudaError_t launch_step_tile<float>(const float* phi_in, float* phi_out, __nv_bfloat16* comp, int comp_mode,
                                         const StepParams& p, int noise_mode, const float* injected, int groups,
-                                        cudaStream_t stream)
+                                        bool rows28, cudaStream_t stream)
     {
         if (comp_mode == COMP_BF16)
-            return by_threads<float, COMP_BF16>(phi_in, phi_out, comp, p, noise_mode, injected, groups, stream);
-        return by_threads<float, COMP_NONE>(phi_in, phi_out, nullptr, p, noise_mode, injected, groups, stream);
+            return by_shape<float, COMP_BF16>(phi_in, phi_out, comp, p, noise_mode, injected, groups, rows28, stream);
+        return by_shape<float, COMP_NONE>(phi_in, phi_out, nullptr, p, noise_mode, injected, groups, rows28, stream);
     }
 
     template <>
     cudaError_t launch_steps_tile_persistent<double>(double* a, double* b, __nv_bfloat16* comp, int comp_mode,
                                                      const StepParams& p, int noise_mode, const double* injected,
-                                                     int nsteps, int groups, cudaStream_t stream)
+                                                     int nsteps, int groups, bool rows28, cudaStream_t stream)
     {
         (void)comp;
         if (comp_mode != COMP_NONE) return cudaErrorInvalidValue;
-        return by_threads_persistent<double, COMP_NONE>(a, b, nullptr, p, noise_mode, injected, nsteps, groups, stream);
+        return by_shape_persistent<double, COMP_NONE>(a, b, nullptr, p, noise_mode, injected, nsteps, groups, rows28,
+                                                      stream);
     }
 
     template <>
     cudaError_t launch_steps_tile_persistent<float>(float* a, float* b, __nv_bfloat16* comp, int comp_mode,
                                                     const StepParams& p, int noise_mode, const float* injected,
-                                                    int nsteps, int groups, cudaStream_t stream)
+                                                    int nsteps, int groups, bool rows28, cudaStream_t stream)
     {
         if (comp_mode == COMP_BF16)
-            return by_threads_persistent<float, COMP_BF16>(a, b, comp, p, noise_mode, injected, nsteps, groups, stream);
-        return by_threads_persistent<float, COMP_NONE>(a, b, nullptr, p, noise_mode, injected, nsteps, groups, stream);
+            return by_shape_persistent<float, COMP_BF16>(a, b, comp, p, noise_mode, injected, nsteps, groups, rows28,
+                                                         stream);
+        return by_shape_persistent<float, COMP_NONE>(a, b, nullptr, p, noise_mode, injected, nsteps, groups, rows28,
+                                                     stream);
     }
 }

@@ -81,6 +81,8 @@ def parse_args(argv=None):
                     help="with --kernel sliding: warp pairs per CTA; with --kernel tile: 256-thread groups per CTA")
     ap.add_argument("--persistent", action="store_true",
                     help="with --kernel tile: all steps of a run in one cooperative launch")
+    ap.add_argument("--tile-rows", type=int, default=32, choices=[32, 28],
+                    help="with --kernel tile: output tile height (32 x 32 or 28 x 32 tiles)")
     ap.add_argument("--fused", action="store_true",
                     help="with --kernel sliding: one warp per strip runs every stage (--pairs counts warps)")
     ap.add_argument("--launches", type=int, default=0,
@@ -380,8 +382,8 @@ def run_ours(args, w, rank, world, dist):
     launch = None
     if args.kernel == "sliding" and (args.seg_rows or args.pairs or args.fused):
         launch = {"seg_rows": args.seg_rows, "pairs_per_cta": args.pairs, "fused": args.fused}
-    elif args.kernel == "tile" and (args.pairs or args.persistent):
-        launch = {"pairs_per_cta": args.pairs, "persistent": args.persistent}
+    elif args.kernel == "tile" and (args.pairs or args.persistent or args.tile_rows != 32):
+        launch = {"pairs_per_cta": args.pairs, "persistent": args.persistent, "tile_rows": args.tile_rows}
     sim = Integrator(field, stencil, model, precision=args.precision, seed=1000 + rank, kernel=args.kernel,
                      launch=launch)
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
@@ -497,14 +499,16 @@ def run_launches(args, w):
     m = N.amb_model(w["a"], w["b"], w["c"], w["kappa"], w["lamb"], w["zeta"], w["T"])
     stream = torch.cuda.current_stream().cuda_stream
     if args.precision == "f64":
-        cfg = N.amb_kernel_config(1, 0, args.pairs, N.AMB_FLAG_PERSISTENT if args.persistent else 0)
+        cfg = N.amb_kernel_config(1, 0, args.pairs, (N.AMB_FLAG_PERSISTENT if args.persistent else 0)
+                                  | (N.AMB_FLAG_TILE_ROWS_28 if args.tile_rows == 28 else 0))
         rc = L.amb_step_f64_ex(ctypes.byref(s), ctypes.byref(m), 1, w["ny"], w["nx"], a.data_ptr(), b.data_ptr(), 0,
                                args.launches, None, ctypes.byref(cfg), stream, None)
     else:
         res = torch.zeros(a.shape, dtype=torch.int16, device="cuda") if args.precision == "f32c" else None
         cfg = N.amb_kernel_config({"auto": 0, "tile": 1, "sliding": 2}[args.kernel], args.seg_rows, args.pairs,
                                   (N.AMB_FLAG_PERSISTENT if args.persistent else 0)
-                                  | (N.AMB_FLAG_FUSED if args.fused else 0))
+                                  | (N.AMB_FLAG_FUSED if args.fused else 0)
+                                  | (N.AMB_FLAG_TILE_ROWS_28 if args.tile_rows == 28 else 0))
         rc = L.amb_step_f32_ex(ctypes.byref(s), ctypes.byref(m), 1, w["ny"], w["nx"], a.data_ptr(), b.data_ptr(),
                                res.data_ptr() if res is not None else None, 0, args.launches, None, ctypes.byref(cfg),
                                stream, None)

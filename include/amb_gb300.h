@@ -89,7 +89,10 @@ typedef struct amb_model
  *   per step costs more than the step; ignored while the stream is being captured). The
  *   results are bitwise those of one launch per step.
  *   AMB_FLAG_FUSED (sliding kernel): one warp per strip runs every stage (no producer/consumer
- *   warp pair); pairs_per_cta then counts warps per CTA (1, 2 or 4). Bitwise the same results. */
+ *   warp pair); pairs_per_cta then counts warps per CTA (1, 2 or 4). Bitwise the same results.
+ *   AMB_FLAG_TILE_ROWS_28 (tile kernel): output tiles of 28 rows x 32 columns instead of 32 x 32
+ *   (balances small grids over the SMs: 512 x 512 is 304 tiles, two per SM). Bitwise the same
+ *   results. */
 typedef struct amb_kernel_config
 {
     int kernel;
@@ -99,6 +102,7 @@ typedef struct amb_kernel_config
 } amb_kernel_config;
 #define AMB_FLAG_PERSISTENT 1
 #define AMB_FLAG_FUSED 2
+#define AMB_FLAG_TILE_ROWS_28 4
 
 /* Number of FP64 planes written by amb_terms_*: mu_p, mu_a, J_p(y,x), J_l(y,x), J_c(y,x), J_r(y,x). */
 #define AMB_NTERMS 10

@@ -157,8 +157,9 @@ def test_autotuner_choice_is_used_and_cached():
 
 
 def test_integrator_explicit_launch_shape():
-    """Integrator(kernel="sliding", launch=...) runs the given launch shape: bitwise equal to the
-    device-pointer call with the same configuration."""
+    """Integrator(kernel="sliding" or "tile", launch=...) runs the given launch shape: bitwise
+    equal to the device-pointer call with the same configuration; a tile height other than 32
+    or 28 is refused."""
     from activemodelbplus.integrator import Integrator, Model, Stencil
     p = Params(T=0.05, **AMB)
     field = initial((96, 448), seed=13)
@@ -167,6 +168,14 @@ def test_integrator_explicit_launch_shape():
     sim.run(10)
     ref = run_f32(field, p, 10, kernel=2, seg_rows=16, pairs=4, comp=False, seed=7)
     assert np.array_equal(sim.field, ref)
+    tile = Integrator(field, Stencil(p.dt, p.dx, p.dy), Model(p.a, p.b, p.c, p.kappa, p.lamb, p.zeta, p.T),
+                      precision="f32", seed=7, kernel="tile",
+                      launch={"pairs_per_cta": 2, "persistent": True, "tile_rows": 28})
+    tile.run(10)
+    assert np.array_equal(tile.field, ref)
+    with pytest.raises(ValueError):
+        Integrator(field, Stencil(p.dt, p.dx, p.dy), Model(p.a, p.b, p.c, p.kappa, p.lamb, p.zeta, p.T),
+                   precision="f32", kernel="tile", launch={"tile_rows": 24})
 
 
 def test_kernels_match_pinned_bits():
@@ -192,9 +201,9 @@ def test_kernels_match_pinned_bits():
 @pytest.mark.parametrize("shape", [(256, 256), (100, 72), (33, 17), (512, 512), (64, 1000)])
 @pytest.mark.parametrize("groups", [1, 2, 4])
 def test_tile_thread_groups_and_persistent_launch_are_bitwise(shape, groups):
-    """256/512/1024 threads per CTA, one launch per step or all steps in one cooperative launch
-    (grid barrier between steps): bitwise the single-step 256-thread result, for odd and even
-    step counts (the result ends in either buffer)."""
+    """256/512/1024 threads per CTA, 32 x 32 or 28 x 32 output tiles, one launch per step or all
+    steps in one cooperative launch (grid barrier between steps): bitwise the single-step
+    256-thread 32 x 32 result, for odd and even step counts (the result ends in either buffer)."""
     field = initial(shape, seed=shape[1])
     p = Params(T=0.05, **AMB)
     for comp in (False, True):
@@ -202,11 +211,14 @@ def test_tile_thread_groups_and_persistent_launch_are_bitwise(shape, groups):
             ref = run_f32(field, p, nsteps, kernel=1, comp=comp)
             assert np.array_equal(run_f32(field, p, nsteps, kernel=1, pairs=groups, comp=comp), ref)
             assert np.array_equal(run_f32(field, p, nsteps, kernel=1, pairs=groups, flags=1, comp=comp), ref)
+            # 28 x 32 output tiles (AMB_FLAG_TILE_ROWS_28), per step and persistent
+            assert np.array_equal(run_f32(field, p, nsteps, kernel=1, pairs=groups, flags=4, comp=comp), ref)
+            assert np.array_equal(run_f32(field, p, nsteps, kernel=1, pairs=groups, flags=5, comp=comp), ref)
 
 
 def test_tile_persistent_injected_noise_and_fp64():
-    """The persistent launch with host-injected noise (one pair of planes per step) and in FP64:
-    bitwise one launch per step."""
+    """The persistent launch and the 28 x 32 tiles with host-injected noise (one pair of planes
+    per step) and in FP64: bitwise one 32 x 32 launch per step."""
     import torch
     N = native()
     rng = np.random.default_rng(21)
@@ -215,11 +227,15 @@ def test_tile_persistent_injected_noise_and_fp64():
     p = Params(T=0.05, **AMB)
     ref = run_f32(field, p, 7, kernel=1, comp=True, injected=noise)
     assert np.array_equal(run_f32(field, p, 7, kernel=1, comp=True, injected=noise, flags=1, pairs=2), ref)
+    for flags in (4, 5):  # 28 x 32 tiles
+        assert np.array_equal(run_f32(field, p, 7, kernel=1, comp=True, injected=noise, flags=flags, pairs=2), ref)
     s = N.amb_stencil(p.dt, p.dx, p.dy)
     m = N.amb_model(p.a, p.b, p.c, p.kappa, p.lamb, p.zeta, p.T)
     stream = torch.cuda.current_stream().cuda_stream
     outs = []
-    for cfg in (None, N.amb_kernel_config(1, 0, 2, N.AMB_FLAG_PERSISTENT)):
+    for cfg in (None, N.amb_kernel_config(1, 0, 2, N.AMB_FLAG_PERSISTENT),
+                N.amb_kernel_config(1, 0, 2, N.AMB_FLAG_TILE_ROWS_28),
+                N.amb_kernel_config(1, 0, 4, N.AMB_FLAG_TILE_ROWS_28 | N.AMB_FLAG_PERSISTENT)):
         a = torch.from_numpy(field.copy()).cuda()
         b = torch.empty_like(a)
         flag = ctypes.c_int(0)
@@ -227,7 +243,8 @@ def test_tile_persistent_injected_noise_and_fp64():
                                      None, ctypes.byref(cfg) if cfg is not None else None, stream, ctypes.byref(flag))
         assert rc == 0, N.last_error()
         outs.append((b if flag.value else a).cpu().numpy())
-    assert np.array_equal(outs[0], outs[1])
+    for o in outs[1:]:
+        assert np.array_equal(outs[0], o)
 
 
 # ------------------------------------------------- the fused (one warp per strip) form
