@@ -51,8 +51,26 @@ namespace amb
         else return *p;
     }
 
+    // Work over a W-wide, H-tall index box by the CTA's NT threads: thread t owns column t % W and
+    // rows t / W, t / W + NT / W, ... (threads past the last whole row of threads idle), so the
+    // index arithmetic is one division per thread and box rather than one per element.
+    template <int W, int H, int NT, typename F>
+    __device__ __forceinline__ void for_box(F&& f)
+    {
+        static_assert(W <= NT, "box wider than the CTA");
+        constexpr int R = NT / W, K = (H + R - 1) / R;
+        const int t = threadIdx.x;
+        if (t < R * W)
+        {
+            const int j = t % W, i0 = t / W;
+#pragma unroll
+            for (int q = 0; q < K; ++q)
+                if (i0 + q * R < H) f(i0 + q * R, j);
+        }
+    }
+
     // One step of one TY x TX output tile (origin r0, c0): the whole body of the tile kernel.
-    template <typename Real, int TY, int TX, int COMP, bool COHERENT>
+    template <typename Real, int TY, int TX, int COMP, bool COHERENT, int NT>
     __device__ __forceinline__ void tile_step(const Real* __restrict__ phi_in, Real* __restrict__ phi_out,
                                               const __nv_bfloat16* comp_in, __nv_bfloat16* comp_out,
                                               const StepParams& p, const Canon<Real>& k, int noise_mode,
@@ -69,57 +87,57 @@ namespace amb
         Real* J1X = J1Y + G::PY * TX;
 
         const int ny = p.ny, nx = p.nx;
-        const int tid = threadIdx.x, nthr = blockDim.x;
+        const int tid = threadIdx.x;
 
-        // Load phi(t) with a 9-site periodic halo: up to 8 loads per thread issued before any of
-        // them is stored, so their latencies overlap.
-        constexpr int NL = G::LY * G::LX, BATCH = 8;
-        for (int base = tid; base < NL; base += BATCH * nthr)
+        // Load phi(t) with a 9-site periodic halo: each thread owns one column of the halo tile
+        // (its periodic image computed once) and issues all its rows' loads before storing any.
         {
-            Real v[BATCH];
-#pragma unroll
-            for (int u = 0; u < BATCH; ++u)
+            constexpr int W = G::LX, R = NT / W, K = (G::LY + R - 1) / R;
+            static_assert(W <= NT, "halo tile wider than the CTA");
+            if (tid < R * W)
             {
-                const int e = base + u * nthr;
-                if (e < NL)
+                const int j = tid % W, i0 = tid / W;
+                const int gc = wrap_index(c0 + j - G::H, nx);
+                Real v[K];
+#pragma unroll
+                for (int q = 0; q < K; ++q)
                 {
-                    const int i = e / G::LX, j = e - i * G::LX;
-                    const int gr = wrap_index(r0 + i - G::H, ny);
-                    const int gc = wrap_index(c0 + j - G::H, nx);
-                    v[u] = load_field<Real, COHERENT>(phi_in + (size_t)gr * nx + gc);
+                    const int i = i0 + q * R;
+                    if (i < G::LY)
+                        v[q] = load_field<Real, COHERENT>(phi_in + (size_t)wrap_index(r0 + i - G::H, ny) * nx + gc);
+                }
+#pragma unroll
+                for (int q = 0; q < K; ++q)
+                {
+                    const int i = i0 + q * R;
+                    if (i < G::LY) PHI[i * G::LX + j] = v[q];
                 }
             }
-#pragma unroll
-            for (int u = 0; u < BATCH; ++u)
-                if (base + u * nthr < NL) PHI[base + u * nthr] = v[u];
         }
         __syncthreads();
 
         // Stage A: mu_p on the (TY+16) x (TX+16) plus-shaped box; mu_a on (TY+4)^2; J_c on (TY+2)^2.
-        for (int e = tid; e < G::MY * G::MX; e += nthr)
-        {
-            int bi = e / G::MX, bj = e - bi * G::MX;      // box coords, offset 8
-            int i = bi - 8, j = bj - 8;                     // tile coords
-            bool in_plus = (i >= 0 && i < TY) || (j >= 0 && j < TX);
-            bool in_a = i >= -2 && i < TY + 2 && j >= -2 && j < TX + 2;
-            if (!in_plus && !in_a) continue;
+        for_box<G::MX, G::MY, NT>([&](int bi, int bj) {  // box coords, offset 8
+            const int i = bi - 8, j = bj - 8;               // tile coords
+            const bool in_plus = (i >= 0 && i < TY) || (j >= 0 && j < TX);
+            const bool in_a = i >= -2 && i < TY + 2 && j >= -2 && j < TX + 2;
+            if (!in_plus && !in_a) return;
+            const int e = bi * G::MX + bj;
             const Real* m = PHI + (i + G::H) * G::LX + (j + G::H);
             if (!in_a)  // the arms of the plus need mu_p only
             {
                 MUP[e] = canon_mu_p(m - G::LX, m, m + G::LX, k);
-                continue;
+                return;
             }
             const SiteA<Real> s = canon_stage_a(m - G::LX, m, m + G::LX, k);
             MUP[e] = s.mup;
+            MUA[(i + 2) * G::AX + (j + 2)] = s.mua;
+            if (i >= -1 && i < TY + 1 && j >= -1 && j < TX + 1)
             {
-                MUA[(i + 2) * G::AX + (j + 2)] = s.mua;
-                if (i >= -1 && i < TY + 1 && j >= -1 && j < TX + 1)
-                {
-                    J2Y[(i + 1) * G::CX + (j + 1)] = s.jcy;
-                    J2X[(i + 1) * G::CX + (j + 1)] = s.jcx;
-                }
+                J2Y[(i + 1) * G::CX + (j + 1)] = s.jcy;
+                J2X[(i + 1) * G::CX + (j + 1)] = s.jcx;
             }
-        }
+        });
         __syncthreads();
 
         // Stage B: J1 = -D8 mu_p + mag xi on the two arms, J2 = -Tj mu_a + J_c on the box. With
@@ -139,28 +157,25 @@ namespace amb
         if (noise_mode == NOISE_PHILOX && nx % 4 == 0)
         {
             constexpr int QY = TX / 4, QQ = G::QX / 4;
-            for (int e = tid; e < G::PY * QY; e += nthr)
-            {
-                int i = e / QY - 4, j = (e % QY) * 4;
+            for_box<QY, G::PY, NT>([&](int ii, int qj) {  // J1_y rows ii - 4, column quad qj
+                const int i = ii - 4, j = qj * 4;
                 float z[4];
                 noise_quad(p.seed, p.step, wrap_index(r0 + i, ny), wrap_index(c0 + j, nx), 0, z);
 #pragma unroll
-                for (int q = 0; q < 4; ++q) J1Y[(i + 4) * TX + j + q] = j1y_at(i, j + q, Real(z[q]));
-            }
-            for (int e = tid; e < TY * QQ; e += nthr)
-            {
-                int i = e / QQ, j = (e % QQ) * 4 - 4;
+                for (int q = 0; q < 4; ++q) J1Y[ii * TX + j + q] = j1y_at(i, j + q, Real(z[q]));
+            });
+            for_box<QQ, TY, NT>([&](int i, int qj) {  // J1_x row i, column quad qj (columns from -4)
+                const int j = qj * 4 - 4;
                 float z[4];
                 noise_quad(p.seed, p.step, wrap_index(r0 + i, ny), wrap_index(c0 + j, nx), 1, z);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) J1X[i * G::QX + j + q + 4] = j1x_at(i, j + q, Real(z[q]));
-            }
+            });
         }
         else
         {
-            for (int e = tid; e < G::PY * TX; e += nthr)
-            {
-                int i = e / TX - 4, j = e % TX;
+            for_box<TX, G::PY, NT>([&](int ii, int j) {
+                const int i = ii - 4;
                 Real xi = 0;
                 if (noise_mode != NOISE_OFF)
                 {
@@ -168,11 +183,10 @@ namespace amb
                     xi = noise_mode == NOISE_PHILOX ? Real(noise_normal(p.seed, p.step, gr, gc, 0))
                                                     : injected[(size_t)gr * nx + gc];
                 }
-                J1Y[e] = j1y_at(i, j, xi);
-            }
-            for (int e = tid; e < TY * G::QX; e += nthr)
-            {
-                int i = e / G::QX, j = e % G::QX - 4;
+                J1Y[ii * TX + j] = j1y_at(i, j, xi);
+            });
+            for_box<G::QX, TY, NT>([&](int i, int jj) {
+                const int j = jj - 4;
                 Real xi = 0;
                 if (noise_mode != NOISE_OFF)
                 {
@@ -180,28 +194,25 @@ namespace amb
                     xi = noise_mode == NOISE_PHILOX ? Real(noise_normal(p.seed, p.step, gr, gc, 1))
                                                     : injected[plane + (size_t)gr * nx + gc];
                 }
-                J1X[e] = j1x_at(i, j, xi);
-            }
+                J1X[i * G::QX + jj] = j1x_at(i, j, xi);
+            });
         }
-        for (int e = tid; e < G::CY * G::CX; e += nthr)
-        {
-            int ci = e / G::CX, cj = e - ci * G::CX;      // box offset 1: rows ci-1..ci+1 of mu_a are its rows ci..ci+2
+        for_box<G::CX, G::CY, NT>([&](int ci, int cj) {
+            const int e = ci * G::CX + cj;
             const Real* a0 = MUA + ci * G::AX + cj + 1;     // mu_a row above, centre column
-            const Real* a1 = a0 + G::AX;
+            const Real* a1 = a0 + G::AX;                    // (box offset 1: rows ci-1..ci+1 of mu_a are its rows ci..ci+2)
             const Real* a2 = a1 + G::AX;
             const Real sx_m = canon_smooth(a0[-1], a0[0], a0[1], k), sx_p = canon_smooth(a2[-1], a2[0], a2[1], k);
             const Real dx_m = rsub(a0[1], a0[-1]), dx_0 = rsub(a1[1], a1[-1]), dx_p = rsub(a2[1], a2[-1]);
             J2Y[e] = canon_j2y(sx_m, sx_p, J2Y[e], k);
             J2X[e] = canon_j2x(dx_m, dx_0, dx_p, J2X[e], k);
-        }
+        });
         __syncthreads();
 
         // Stage C: div J and the update.
-        for (int e = tid; e < TY * TX; e += nthr)
-        {
-            int i = e / TX, j = e - i * TX;
-            int gr = r0 + i, gc = c0 + j;
-            if (gr >= ny || gc >= nx) continue;
+        for_box<TX, TY, NT>([&](int i, int j) {
+            const int gr = r0 + i, gc = c0 + j;
+            if (gr >= ny || gc >= nx) return;
             const Real* y0 = J2Y + i * G::CX + j + 1;       // J2 rows i-1, i, i+1 at J2 rows i, i+1, i+2
             const Real* y2 = y0 + 2 * G::CX;
             const Real* x0 = J2X + i * G::CX + j + 1;
@@ -226,18 +237,19 @@ namespace amb
             {
                 phi_out[gi] = canon_update(f, dx8, divtj, dy8, k);
             }
-        }
+        });
     }
 
-    // One step, one tile per CTA (grid = tiles).
+    // One step, one tile per CTA (grid = tiles). Both tile kernels are built for 1024 threads per
+    // SM (at most 64 registers per thread).
     template <typename Real, int TY, int TX, int COMP, int NT>
-    __global__ void __launch_bounds__(NT)
+    __global__ void __launch_bounds__(NT, 1024 / NT)
     step_tile_kernel(const Real* __restrict__ phi_in, Real* __restrict__ phi_out,
                      const __nv_bfloat16* comp_in, __nv_bfloat16* comp_out,  // may alias: each site reads/writes only its own
                      StepParams p, const Canon<Real> k, int noise_mode, const Real* __restrict__ injected)
     {
         extern __shared__ __align__(16) unsigned char smem_raw[];
-        tile_step<Real, TY, TX, COMP, false>(phi_in, phi_out, comp_in, comp_out, p, k, noise_mode, injected,
+        tile_step<Real, TY, TX, COMP, false, NT>(phi_in, phi_out, comp_in, comp_out, p, k, noise_mode, injected,
                                              blockIdx.y * TY, blockIdx.x * TX, smem_raw);
     }
 
@@ -276,7 +288,7 @@ namespace amb
     // the result is bitwise that of nsteps single-step launches. If a barrier gives up, the CTA
     // fills its tiles of both buffers with NaN (caught by the finite check) and leaves.
     template <typename Real, int TY, int TX, int COMP, int NT>
-    __global__ void __launch_bounds__(NT)
+    __global__ void __launch_bounds__(NT, 1024 / NT)
     step_tile_persistent_kernel(Real* buf0, Real* buf1, __nv_bfloat16* comp, StepParams p, const Canon<Real> k,
                                 int noise_mode, const Real* __restrict__ injected, int nsteps, unsigned* count,
                                 int* error)
@@ -295,7 +307,7 @@ namespace amb
             const Real* inj = injected ? injected + (size_t)s * 2 * plane : nullptr;
             for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
             {
-                tile_step<Real, TY, TX, COMP, true>(in, out, comp, comp, p, k, noise_mode, inj, (tile / tx) * TY,
+                tile_step<Real, TY, TX, COMP, true, NT>(in, out, comp, comp, p, k, noise_mode, inj, (tile / tx) * TY,
                                                     (tile % tx) * TX, smem_raw);
                 __syncthreads();
             }
