@@ -816,7 +816,21 @@ namespace
         for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
         {
             int r, k;
-            if (ks == 1)
+            if (n <= INT32_MAX)  // 32-bit division (a 64-bit one costs several times the instructions)
+            {
+                const int ii = int(i);
+                if (ks == 1)
+                {
+                    r = ii / int(rs);
+                    k = ii - r * int(rs);
+                }
+                else
+                {
+                    k = ii / int(ks);
+                    r = ii - k * int(ks);
+                }
+            }
+            else if (ks == 1)
             {
                 r = int(i / rs);
                 k = int(i - int64_t(r) * rs);
@@ -891,7 +905,7 @@ namespace
                                           uint4* __restrict__ x_next)
     {
         // the next macro step's noise key (nothing in this launch reads it)
-        if (advance && blockIdx.x == 0 && threadIdx.x == 0) *advance += 1;
+        if (advance && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *advance += 1;
         const size_t plane = size_t(nrows) * ncols;
         const float* fy = flux;
         const float* fx = flux + plane;
@@ -899,10 +913,14 @@ namespace
         const float* ex = extra ? extra + plane : nullptr;
         const float* xy = xi;
         const float* xx = xi ? xi + plane : nullptr;
-        for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < plane; i += size_t(gridDim.x) * blockDim.x)
+        // rows by blockIdx.y (grid-stride), columns by blockIdx.x and the thread: no division per site
+        const int c = blockIdx.x * blockDim.x + threadIdx.x;
+        if (c >= ncols) return;
+        const int cm = c == 0 ? ncols - 1 : c - 1;
+        for (int r = blockIdx.y; r < nrows; r += gridDim.y)
         {
-            const int r = int(i / ncols), c = int(i - size_t(r) * ncols);
-            const int rm = r == 0 ? nrows - 1 : r - 1, cm = c == 0 ? ncols - 1 : c - 1;
+            const size_t i = size_t(r) * ncols + c;
+            const int rm = r == 0 ? nrows - 1 : r - 1;
             long long dq = face_q(fx, ex, xx, noise_mag, scale_x, r, c, 0, 1, nrows, ncols) -
                            face_q(fx, ex, xx, noise_mag, scale_x, r, cm, 0, 1, nrows, ncols) +
                            face_q(fy, ey, xy, noise_mag, scale_y, r, c, 1, 0, nrows, ncols) -
@@ -916,7 +934,9 @@ namespace
                 q = q > bound ? bound : (q < -bound ? -bound : q);
             }
             phi_q[i] = int32_t(q);
-            const float f = float(double(q) * (1.0 / 16777216.0));
+            // q * 2^-24 rounded once to FP32: rounding q to FP32 and scaling by a power of two gives the
+            // same value (|q| <= 2e9, so the scaled value is a normal number or zero)
+            const float f = __fmul_rn(__int2float_rn(int(q)), 1.0f / 16777216.0f);
             phi_f[i] = f;
             if (x_next)  // channel chunk 0 of the next network input, as learned_input_kernel forms it
             {
@@ -1173,8 +1193,7 @@ static int learned_update_launch(const float* flux, const float* extra, int nrow
                                  void* stream)
 {
     auto s = static_cast<cudaStream_t>(stream);
-    const size_t n = size_t(nrows) * ncols;
-    const int grid = int(std::min<size_t>((n + 255) / 256, size_t(sm_count()) * 16));
+    const dim3 grid((ncols + 255) / 256, std::min(nrows, 65535));
     const double fix = 16777216.0;
     const double qb = std::min(bound * fix, 2.0e9);
     const bool noisy = xi && noise_mag > 0;
